@@ -1,0 +1,347 @@
+"""Benchmark: the q=26, r=5, fill-0.8 standard quotient filter workload
+(53,687,091 MT19937 keys, seed 2) through the reference's host API.
+
+One step = bulkBuildSegmentedLayouts (NoDup) of all keys, 2^24 unsorted
+lookups, 2^24 sorted lookups (50% inserted keys, 50% fresh draws), an
+insert of 2^20 fresh keys and 2^20 deletes of present keys.  `value` is the
+step's operations (keys built + queries + inserts + deletes) per second of
+device time, summed over ranks (each rank runs an independent filter:
+replicas, weak scaling).  Every op is timed on its stream with CUDA events,
+with L2 flushed before each op.  `e2e` repeats the step through the same API
+from pinned host buffers, host<->device copies inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "M ops/s build/lookup/insert at q=26 r=5 fill .8 (%HBM roofline); served p50/p99"
+Q, R, SEED = 26, 5, 2
+N_KEYS = 53687091
+N_LOOKUP = 1 << 24
+N_INSERT = 1 << 20
+N_DELETE = 1 << 20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(op: str, n: int, T: int) -> float:
+    """Bytes one op must move at minimum (per-op model of the design notes)."""
+    if op == "build":
+        return 12.0 * n + T       # keys in, one fingerprint permutation, table out
+    if op == "lookup_unsorted":
+        return 40.0 * n           # key + result + one 32-B table sector
+    if op == "lookup_sorted":
+        return 24.0 * n + T       # key + result + (fp, idx) pair out and back + table sweep
+    return 68.0 * n               # insert / delete: key + one sector read + written
+
+
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(
+                        ["nvidia-smi", "-i", str(self.index),
+                         "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                         "clocks_event_reasons.sw_power_cap",
+                         "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                    if out.returncode == 0 and out.stdout.strip():
+                        self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 2 + i and "Active" in r[2 + i]
+                          and r[2 + i] != "Not Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        import torch
+        if not torch.cuda.is_available():
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, world, rank, local):
+    import torch
+
+    import gpuquotientfilters_gb300 as G
+    from gpuquotientfilters_gb300 import workload as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    G.lib()
+    c = W.config2(seed=SEED + 0 * rank)
+    T = G.calcNumSlotsGPU(Q, R)
+
+    def dev_u32(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
+
+    d_keys = dev_u32(c["keys"])
+    d_look = dev_u32(c["lookups"])
+    d_ins = dev_u32(c["inserts"])
+    d_del = dev_u32(c["deletes"])
+    d_out = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
+    d_out2 = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    qf = G.initFilterGPU(Q, R)
+    stream = torch.cuda.current_stream(dev)
+
+    ops = [
+        ("build", N_KEYS, lambda: G.bulkBuildSegmentedLayouts(qf, N_KEYS, d_keys, True, stream=stream)),
+        ("lookup_unsorted", N_LOOKUP, lambda: G.launchUnsortedLookups(qf, N_LOOKUP, d_look, d_out, stream=stream)),
+        ("lookup_sorted", N_LOOKUP, lambda: G.launchSortedLookups(qf, N_LOOKUP, d_look, d_out2, stream=stream)),
+        ("insert", N_INSERT, lambda: G.insert(qf, N_INSERT, d_ins, stream=stream)),
+        ("delete", N_DELETE, lambda: G.superclusterDeletes(qf, N_DELETE, d_del, stream=stream)),
+    ]
+
+    def step(record):
+        tot = 0.0
+        for name, n, fn in ops:
+            flush.fill_(1)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            fn()
+            ev1.record(stream)
+            ev1.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            tot += ms
+            if record is not None:
+                record.setdefault(name, []).append(ms)
+        return tot
+
+    for _ in range(args.warmup):
+        step(None)
+    # correctness guard on the measured path: sorted == unsorted
+    assert torch.equal(d_out, d_out2), "sorted and unsorted lookups disagree"
+
+    clocks = ClockSampler(local)
+    rec = {}
+    launches0 = G.lib().gqf_kernel_launches()
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    t_dev = 0.0
+    for _ in range(args.steps):
+        t_dev += step(rec)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop()
+    launches = G.lib().gqf_kernel_launches() - launches0
+    t_max = max_over_ranks(world, t_dev, dev)
+    ops_per_step = sum(n for _, n, _ in ops)
+    value = world * ops_per_step * args.steps / (t_max / 1e3) / 1e6
+    peak, peak_kind = peaks()
+    per_op = {}
+    for name, n, _ in ops:
+        ms = float(np.mean(rec[name]))
+        gbs = algorithmic_bytes(name, n, T) / (ms / 1e3) / 1e9
+        per_op[name] = {"n": n, "ms": round(ms, 4), "mops": round(n / ms / 1e3, 1),
+                        "alg_GBps": round(gbs, 1), "frac_hbm": round(gbs / peak, 4)}
+    b = per_op["build"]
+
+    # end to end through the same API from pinned host buffers
+    e2e = e2e_step(args, G, torch, dev, stream, c, qf)
+    G.freeFilterGPU(qf)
+    return {
+        "value": value, "ms_per_step": t_max / args.steps, "per_op": per_op, "clocks": clk,
+        "gpu_launches": int(launches), "peak": peak, "peak_kind": peak_kind, "e2e": e2e,
+        "roofline": {"bound": "hbm", "kernel": "bulk build pipeline (hash+bucket scatter, bucket layout, fixup)",
+                     "achieved": b["alg_GBps"], "peak": peak, "unit": "GB/s", "frac": b["frac_hbm"],
+                     "traffic": None, "peak_source": peak_kind},
+    }
+
+
+def e2e_step(args, G, torch, dev, stream, c, qf):
+    """The same step from pinned host memory: copies in, ops, results out."""
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).pin_memory()
+
+    h_keys, h_look, h_ins, h_del = pinned(c["keys"]), pinned(c["lookups"]), pinned(c["inserts"]), pinned(c["deletes"])
+    h_out = torch.empty(N_LOOKUP, dtype=torch.int32).pin_memory()
+    h_out2 = torch.empty(N_LOOKUP, dtype=torch.int32).pin_memory()
+    d_keys = torch.empty(N_KEYS, dtype=torch.int32, device=dev)
+    d_look = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
+    d_ins = torch.empty(N_INSERT, dtype=torch.int32, device=dev)
+    d_del = torch.empty(N_DELETE, dtype=torch.int32, device=dev)
+    d_out = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
+    d_out2 = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
+    bi = 4 * (N_KEYS + N_LOOKUP + N_INSERT + N_DELETE)
+    bo = 4 * 2 * N_LOOKUP
+
+    def one():
+        d_keys.copy_(h_keys, non_blocking=True)
+        G.bulkBuildSegmentedLayouts(qf, N_KEYS, d_keys, True, stream=stream)
+        d_look.copy_(h_look, non_blocking=True)
+        G.launchUnsortedLookups(qf, N_LOOKUP, d_look, d_out, stream=stream)
+        h_out.copy_(d_out, non_blocking=True)
+        G.launchSortedLookups(qf, N_LOOKUP, d_look, d_out2, stream=stream)
+        h_out2.copy_(d_out2, non_blocking=True)
+        d_ins.copy_(h_ins, non_blocking=True)
+        G.insert(qf, N_INSERT, d_ins, stream=stream)
+        d_del.copy_(h_del, non_blocking=True)
+        G.superclusterDeletes(qf, N_DELETE, d_del, stream=stream)
+
+    for _ in range(max(1, args.warmup)):
+        one()
+    torch.cuda.synchronize(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        one()
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ops = N_KEYS + 2 * N_LOOKUP + N_INSERT + N_DELETE
+    return {"value": ops / ms / 1e3, "unit": "M ops/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
+            "ms_per_step": ms}
+
+
+# -------------------------------------------------------------- CPU baseline
+CPU_SAMPLE = dict(n_build=8 << 20, n_lookup=4 << 20, n_insert=1 << 20, n_delete=1 << 20)
+
+
+def cpu_sample_run(sample=CPU_SAMPLE):
+    """The oracle port (sequential CPU algorithm of the reference's
+    CPU_version, GPU hash) on a bounded sample of the same workload: build by
+    sequential insertItem of the first n_build keys into a q=26 table, then
+    lookups, inserts and deletes.  Returns (M ops/s, seconds, description)."""
+    import oracle as O
+    from gpuquotientfilters_gb300 import workload as W
+    keys = O.mt_keys(SEED, sample["n_build"])
+    look = W.mixed_lookups(keys, sample["n_lookup"], SEED, skip=N_KEYS + N_INSERT)
+    ins = O.mt_keys(SEED, sample["n_insert"], skip=N_KEYS)
+    dels = keys[: sample["n_delete"]]
+    t = O.sqf_new(Q, R)
+    t0 = time.perf_counter()
+    O.sqf_insert(t, Q, R, keys)
+    O.sqf_lookup(t, Q, R, look)
+    O.sqf_insert(t, Q, R, ins)
+    O.sqf_delete(t, Q, R, dels)
+    dt = time.perf_counter() - t0
+    nops = sum(sample.values())
+    desc = ("oracle port, 1 thread: insertItem of %d keys into a q=26 r=5 table, %d lookups, %d inserts, "
+            "%d deletes" % (sample["n_build"], sample["n_lookup"], sample["n_insert"], sample["n_delete"]))
+    return nops / dt / 1e6, dt, desc
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    import oracle as O
+    O.build()
+    sample = dict(n_build=2 << 20, n_lookup=1 << 20, n_insert=1 << 18, n_delete=1 << 18)
+    for _ in range(args.warmup):
+        cpu_sample_run(sample)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, dt, desc = cpu_sample_run(sample)
+        vals.append(v)
+        secs += dt
+    value = float(np.mean(vals))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "M ops/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "SQF q=26 r=5 fill 0.8 (MT19937 seed 2), CPU sample per step", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "M ops/s", "cores": 1, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": "M ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gqf", choices=["gqf", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    r = run_gpu(args, world, rank, local)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt, desc = cpu_sample_run()
+        cpu = {"value": v, "unit": "M ops/s", "cores": 1, "kind": "port", "sample": desc, "seconds": round(dt, 2)}
+    out = {
+        "metric": METRIC, "value": r["value"], "unit": "M ops/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (MT19937 seed 2 keys)",
+        "config": {"workload": "SQF q=26 r=5 fill 0.8: build 53,687,091 keys NoDup + 2^24 unsorted + 2^24 sorted "
+                               "lookups (50% positive) + 2^20 inserts + 2^20 deletes",
+                   "q": Q, "r": R, "n_keys": N_KEYS, "l2": "flushed (256 MB write) before every op",
+                   "parallelism": "replicas x%d" % world},
+        "per_op": r["per_op"], "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"],
+        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"],
+    }
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

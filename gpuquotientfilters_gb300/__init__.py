@@ -1,0 +1,305 @@
+"""GB300 quotient-filter engine: Python mirror of the reference host API.
+
+The functions below carry the names, argument meaning and return value
+(elapsed milliseconds) of owensgroup/GPUQuotientFilters'
+``quotientFilter.cuh`` and ``RSQF.cuh``; they call the C ABI of
+``libgqf.so`` (declared in ``include/gqf.h``) through ctypes.  Device
+buffers are passed as CUDA tensors (or raw integer device pointers); torch
+only provides the memory and streams.
+
+Where the reference prints and carries on (or aborts), these raise
+``GQFError`` with the library's status.  There is no CPU fallback: if
+``libgqf.so`` cannot be loaded, importing a compute entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgqf.so")
+NOT_FOUND = 0xFFFFFFFF
+RBITS = 5
+SLOTS_PER_BLOCK = 64
+
+GQF_OK, GQF_ERR_ARG, GQF_ERR_FULL, GQF_ERR_CUDA, GQF_ERR_TIMEOUT, GQF_ERR_NOMEM, GQF_ERR_MISMATCH = range(7)
+
+
+class GQFError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__("%s: %s (status %d)" % (what, _lib().gqf_status_string(status).decode(), status))
+
+
+class quotient_filter(C.Structure):
+    """struct quotient_filter (quotientFilter.cuh:25-31)."""
+    _fields_ = [("qbits", C.c_uint), ("rbits", C.c_uint), ("bytesPerElement", C.c_uint),
+                ("table", C.c_void_p)]
+
+
+class countingQuotientFilterGPU(C.Structure):
+    """struct countingQuotientFilterGPU (RSQF.cuh:32-37)."""
+    _fields_ = [("qbits", C.c_uint), ("numBlocks", C.c_uint), ("blocks", C.c_void_p)]
+
+
+_L = None
+
+
+def build(force: bool = False) -> str:
+    """Compiles libgqf.so in-tree for sm_103a (see buildlib.py)."""
+    from . import buildlib
+    return buildlib.build(force=force)
+
+
+def _lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libgqf.so is not built: run gpuquotientfilters_gb300.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, i32, f32p = C.c_void_p, C.c_uint32, C.c_int, C.POINTER(C.c_float)
+        qfp = C.POINTER(quotient_filter)
+        cqfp = C.POINTER(countingQuotientFilterGPU)
+        sig = {
+            "gqf_sqf_table_bytes": (C.c_size_t, [C.c_uint, C.c_uint]),
+            "gqf_sqf_num_slots": (C.c_uint, [C.c_uint]),
+            "gqf_aphash": (C.c_uint, [C.c_uint, C.c_uint]),
+            "gqf_rsqf_num_blocks": (C.c_size_t, [C.c_uint]),
+            "gqf_mt19937_fill": (None, [u32, C.c_uint64, vp, C.c_uint64]),
+            "gqf_status_string": (C.c_char_p, [i32]),
+            "gqf_stream_status": (i32, [vp]),
+            "gqf_sqf_init": (i32, [qfp, C.c_uint, C.c_uint]),
+            "gqf_sqf_free": (i32, [qfp]),
+            "gqf_sqf_bulk_build": (i32, [qfp, i32, vp, i32, vp, f32p]),
+            "gqf_sqf_lookup_unsorted": (i32, [qfp, i32, vp, vp, vp, f32p]),
+            "gqf_sqf_lookup_sorted": (i32, [qfp, i32, vp, vp, vp, f32p]),
+            "gqf_sqf_insert": (i32, [qfp, i32, vp, vp, f32p]),
+            "gqf_sqf_delete": (i32, [qfp, i32, vp, vp, f32p]),
+            "gqf_sqf_insert_via_merge": (i32, [qfp, vp, i32, vp, i32, i32, vp, f32p]),
+            "gqf_sqf_merge": (i32, [qfp, qfp, i32, vp, f32p]),
+            "gqf_rsqf_init": (i32, [cqfp, C.c_uint]),
+            "gqf_rsqf_free": (i32, [cqfp]),
+            "gqf_rsqf_insert": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_rsqf_lookup_sorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_rsqf_lookup_unsorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _L = L
+    return _L
+
+
+def lib():
+    """The loaded libgqf.so (ctypes.CDLL)."""
+    return _lib()
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    return int(x.data_ptr())
+
+
+def _stream_ptr(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)
+
+
+def _check(st: int, what: str):
+    if st != GQF_OK:
+        raise GQFError(st, what)
+
+
+def _timed(fn, *args, stream=None):
+    ms = C.c_float(0.0)
+    st = fn(*args, _stream_ptr(stream), C.byref(ms))
+    _check(st, fn.__name__)
+    return ms.value
+
+
+# ------------------------------------------------------------- host helpers
+def calcNumSlotsGPU(q: int, r: int) -> int:
+    """Table bytes (quotientFilter.cu:37-42)."""
+    return int(_lib().gqf_sqf_table_bytes(q, r))
+
+
+def num_slots(q: int) -> int:
+    return int(_lib().gqf_sqf_num_slots(q))
+
+
+def Normal_APHash(value: int, tableSize: int) -> int:
+    return int(_lib().gqf_aphash(value, tableSize))
+
+
+Normal_APHashGPU = Normal_APHash
+
+
+def calcNumBlocksGPU(q: int) -> int:
+    return int(_lib().gqf_rsqf_num_blocks(q))
+
+
+def mt19937(seed: int, n: int, skip: int = 0):
+    """n draws of genrand_int32 after init_genrand(seed) (numpy uint32)."""
+    import numpy as np
+    out = np.empty(n, np.uint32)
+    _lib().gqf_mt19937_fill(seed, skip, out.ctypes.data, n)
+    return out
+
+
+# --------------------------------------------------- standard quotient filter
+def initFilterGPU(q: int, r: int) -> quotient_filter:
+    qf = quotient_filter()
+    _check(_lib().gqf_sqf_init(C.byref(qf), q, r), "initFilterGPU")
+    return qf
+
+
+def freeFilterGPU(qf: quotient_filter) -> None:
+    _check(_lib().gqf_sqf_free(C.byref(qf)), "freeFilterGPU")
+
+
+def bulkBuildSegmentedLayouts(qf, numValues, d_insertValues, NoDuplicates, stream=None) -> float:
+    return _timed(_lib().gqf_sqf_bulk_build, C.byref(qf), int(numValues), _ptr(d_insertValues),
+                  int(bool(NoDuplicates)), stream=stream)
+
+
+# The reference's other two bulk builds produce the same (canonical) table.
+bulkBuildParallelMerging = bulkBuildSegmentedLayouts
+bulkBuildSequentialShifts = bulkBuildSegmentedLayouts
+
+
+def launchUnsortedLookups(qf, numValues, d_lookupValues, d_returnValues, stream=None) -> float:
+    return _timed(_lib().gqf_sqf_lookup_unsorted, C.byref(qf), int(numValues), _ptr(d_lookupValues),
+                  _ptr(d_returnValues), stream=stream)
+
+
+def launchSortedLookups(qf, numValues, d_lookupValues, d_returnValues, stream=None) -> float:
+    return _timed(_lib().gqf_sqf_lookup_sorted, C.byref(qf), int(numValues), _ptr(d_lookupValues),
+                  _ptr(d_returnValues), stream=stream)
+
+
+def insert(qf, numValues, d_insertValues, stream=None) -> float:
+    return _timed(_lib().gqf_sqf_insert, C.byref(qf), int(numValues), _ptr(d_insertValues), stream=stream)
+
+
+def superclusterDeletes(qf, numValues, d_deleteValues, stream=None) -> float:
+    return _timed(_lib().gqf_sqf_delete, C.byref(qf), int(numValues), _ptr(d_deleteValues), stream=stream)
+
+
+def insertViaMerge(qf, d_insertedValues, numOldValues, d_newValues, numNewValues, NoDuplicates,
+                   stream=None) -> float:
+    return _timed(_lib().gqf_sqf_insert_via_merge, C.byref(qf), _ptr(d_insertedValues), int(numOldValues),
+                  _ptr(d_newValues), int(numNewValues), int(bool(NoDuplicates)), stream=stream)
+
+
+def mergeTwoFilters(qf1, qf2, NoDuplicates, stream=None) -> float:
+    return _timed(_lib().gqf_sqf_merge, C.byref(qf1), C.byref(qf2), int(bool(NoDuplicates)), stream=stream)
+
+
+def table_bytes(qf):
+    """Host copy of the table (numpy uint8), for inspection and tests."""
+    import numpy as np
+    n = calcNumSlotsGPU(qf.qbits, qf.rbits)
+    host = np.empty(n, np.uint8)
+    _memcpy_d2h(host.ctypes.data, qf.table, n)
+    return host
+
+
+def _memcpy_d2h(dst: int, src: int, nbytes: int):
+    st = _cudart().cudaMemcpy(C.c_void_p(dst), C.c_void_p(src), C.c_size_t(nbytes), 2)
+    if st != 0:
+        raise RuntimeError("cudaMemcpy failed: %d" % st)
+
+
+def _memcpy_h2d(dst: int, src: int, nbytes: int):
+    st = _cudart().cudaMemcpy(C.c_void_p(dst), C.c_void_p(src), C.c_size_t(nbytes), 1)
+    if st != 0:
+        raise RuntimeError("cudaMemcpy failed: %d" % st)
+
+
+_CUDART = None
+
+
+def _cudart():
+    global _CUDART
+    if _CUDART is None:
+        import glob
+        import torch  # noqa: F401  (loads the CUDA runtime torch ships)
+        cands = []
+        for d in [os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")]:
+            cands += sorted(glob.glob(os.path.join(d, "libcudart.so*")))
+        L = None
+        for c in cands + ["libcudart.so", "libcudart.so.13", "libcudart.so.12"]:
+            try:
+                L = C.CDLL(c)
+                break
+            except OSError:
+                continue
+        if L is None:
+            raise OSError("libcudart not found")
+        L.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        L.cudaMemcpy.restype = C.c_int
+        _CUDART = L
+    return _CUDART
+
+
+def printQuotientFilterGPU(qf) -> None:
+    """printQuotientFilterGPU (quotientFilter.cu:383-405): metadata row then
+    remainder row, ten slots per line."""
+    t = table_bytes(qf)
+    bpe = qf.bytesPerElement
+    n = num_slots(qf.qbits)
+    print("Printing metadata and remainders:")
+    for i in range(n // 10):
+        els = []
+        for j in range(10):
+            k = (10 * i + j) * bpe
+            e = 0
+            for b in range(bpe):
+                e = (e << 8) | int(t[k + b])
+            els.append(e)
+        print("".join("%u \t" % (e & 7) for e in els))
+        print("".join("%u \t" % (e >> 3) for e in els))
+        print(" --------------------------------------------------------------------- ")
+    print()
+
+
+# ----------------------------------------- rank-and-select quotient filter
+def initCQFGPU(q: int) -> countingQuotientFilterGPU:
+    cqf = countingQuotientFilterGPU()
+    _check(_lib().gqf_rsqf_init(C.byref(cqf), q), "initCQFGPU")
+    return cqf
+
+
+def freeCQFGPU(cqf) -> None:
+    _check(_lib().gqf_rsqf_free(C.byref(cqf)), "freeCQFGPU")
+
+
+def insertGPU(cqf, numValues, d_insertValues, d_returnValues, stream=None) -> float:
+    return _timed(_lib().gqf_rsqf_insert, C.byref(cqf), int(numValues), _ptr(d_insertValues),
+                  _ptr(d_returnValues), stream=stream)
+
+
+def launchLookups(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None) -> float:
+    return _timed(_lib().gqf_rsqf_lookup_sorted, C.byref(cqf), int(numValues), _ptr(d_lookupValues),
+                  _ptr(d_slotValuesArray), stream=stream)
+
+
+def launchUnsortedLookupsRSQF(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None) -> float:
+    return _timed(_lib().gqf_rsqf_lookup_unsorted, C.byref(cqf), int(numValues), _ptr(d_lookupValues),
+                  _ptr(d_slotValuesArray), stream=stream)
+
+
+def rsqf_blocks_bytes(cqf):
+    """Host copy of the packed blocks (numpy uint8), guard block included."""
+    import numpy as np
+    n = (cqf.numBlocks + 1) * 57
+    host = np.empty(n, np.uint8)
+    _memcpy_d2h(host.ctypes.data, cqf.blocks, n)
+    return host

@@ -1,0 +1,138 @@
+// Device-side building blocks shared by the SQF and RSQF kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gqf.h"
+
+#define QF_HD __host__ __device__ __forceinline__
+
+namespace gqf {
+
+// Device error word bits (latched per stream by the host layer).
+enum : uint32_t {
+    DEV_ERR_FULL = 1u,          // a layout ran past (1<<q)*1.1 slots
+    DEV_ERR_TIMEOUT = 2u,       // a bounded spin-wait gave up
+    DEV_ERR_BUCKET_OVER = 4u,   // speculative bucket capacity exceeded (host retries)
+    DEV_ERR_BUCKET_CAP = 8u,    // a bucket is larger than one CTA can sort (host falls back)
+};
+
+// Normal_APHash without the final modulo (quotientFilter.cu:134-149):
+// four byte rounds, most significant byte first.  Callers mask to q+r bits,
+// which equals `% (1 << (q+r))`.
+QF_HD uint32_t aphash32(uint32_t v)
+{
+    uint32_t h = 0xAAAAAAAAu;
+    h ^= (h << 7) ^ (v >> 24) ^ (h >> 3);
+    h ^= ~((h << 11) ^ ((v >> 16) & 0xFFu) ^ (h >> 5));
+    h ^= (h << 7) ^ ((v >> 8) & 0xFFu) ^ (h >> 3);
+    h ^= ~((h << 11) ^ (v & 0xFFu) ^ (h >> 5));
+    return h;
+}
+
+// Slot element: rem << 3 | occupied << 2 | continuation << 1 | shifted
+// (quotientFilter.cu:57-115).
+QF_HD bool e_occ(uint32_t e) { return (e >> 2) & 1u; }
+QF_HD bool e_cont(uint32_t e) { return (e >> 1) & 1u; }
+QF_HD bool e_shift(uint32_t e) { return e & 1u; }
+QF_HD bool e_empty(uint32_t e) { return (e & 7u) == 0; }
+
+// ---- SWAR over 8 one-byte slots held in a little-endian u64 ----------
+// bit k of the result = bit 0 of byte k
+QF_HD uint32_t pack8(uint64_t x)
+{
+    x &= 0x0101010101010101ull;
+    return (uint32_t)((x * 0x0102040810204080ull) >> 56);
+}
+struct Flags8 {
+    uint32_t occ, cont, shift, nonempty;
+};
+QF_HD Flags8 flags8(uint64_t x)
+{
+    Flags8 f;
+    f.occ = pack8(x >> 2);
+    f.cont = pack8(x >> 1);
+    f.shift = pack8(x);
+    f.nonempty = pack8(x | (x >> 1) | (x >> 2));
+    return f;
+}
+
+QF_HD int popc32(uint32_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+QF_HD int highest_bit(uint32_t x)  // x != 0
+{
+#ifdef __CUDA_ARCH__
+    return 31 - __clz(x);
+#else
+    return 31 - __builtin_clz(x);
+#endif
+}
+QF_HD int lowest_bit(uint32_t x)  // x != 0
+{
+#ifdef __CUDA_ARCH__
+    return __ffs(x) - 1;
+#else
+    return __builtin_ctz(x);
+#endif
+}
+// position of the j-th (0-based) set bit of m; m has more than j set bits
+QF_HD int select_bit(uint32_t m, int j)
+{
+    for (int i = 0; i < j; i++) m &= m - 1;
+    return lowest_bit(m);
+}
+
+// ---- memory-order helpers for the decoupled look-back -------------------
+#ifdef __CUDACC__
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+#endif
+
+// Look-back descriptor (64 bits): [63:62] flag, payload below.
+//   AGG: [61:31] n (items), [30:0] F (end slot when entering at slot 0)
+//   INC: [30:0] c_out (first slot after this bucket's items)
+// A bucket's layout maps an entry slot c to max(c + n, F); composing two
+// buckets (a then b) gives (n_a + n_b, max(F_a + n_b, F_b)).
+constexpr unsigned long long LB_AGG = 1ull << 62;
+constexpr unsigned long long LB_INC = 2ull << 62;
+constexpr uint32_t LB_VMAX = 0x7FFFFFFFu;
+QF_HD unsigned long long lb_pack_agg(uint32_t n, uint32_t F)
+{
+    return LB_AGG | ((unsigned long long)(n & LB_VMAX) << 31) | (F & LB_VMAX);
+}
+QF_HD unsigned long long lb_pack_inc(uint32_t c) { return LB_INC | (c & LB_VMAX); }
+
+struct LayoutFn {
+    uint32_t n, F;  // c -> max(c + n, F)
+    QF_HD uint32_t apply(uint32_t c) const
+    {
+        uint32_t a = c + n;
+        return a > F ? a : F;
+    }
+};
+// first a, then b
+QF_HD LayoutFn compose(LayoutFn a, LayoutFn b)
+{
+    LayoutFn r;
+    r.n = a.n + b.n;
+    uint32_t x = a.F + b.n;
+    r.F = x > b.F ? x : b.F;
+    return r;
+}
+
+}  // namespace gqf

@@ -1,0 +1,487 @@
+// C ABI of the standard quotient filter: host orchestration of the kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+
+#include "host_common.cuh"
+#include "sqf_build.cuh"
+#include "sqf_extract.cuh"
+#include "sqf_lookup.cuh"
+
+namespace gqf {
+
+// ------------------------------------------------------------------ geometry
+static bool qr_ok(unsigned q, unsigned r)
+{
+    // quotientFilter.cu:46-47 asserts q + r <= 32 and (r + 3) % 8 == 0; a
+    // 32-bit fingerprint would need `1 << 32` in the hash modulus (:268), so
+    // q + r <= 31 here.  q >= 7 keeps a bucket at least 128 quotients.
+    return (r + 3) % 8 == 0 && (r + 3) / 8 <= 2 && q >= 7 && q + r <= 31 && r >= 1;
+}
+
+struct SqfGeom {
+    uint32_t q, r, bpe, nslots;
+    size_t T;
+};
+static SqfGeom geom_of(const gqf_sqf *qf)
+{
+    SqfGeom g;
+    g.q = qf->qbits;
+    g.r = qf->rbits;
+    g.bpe = (g.r + 3) / 8;
+    g.nslots = gqf_sqf_num_slots(g.q);
+    g.T = gqf_sqf_table_bytes(g.q, g.r);
+    return g;
+}
+
+static uint32_t ceil_log2(uint64_t x)
+{
+    uint32_t l = 0;
+    while ((1ull << l) < x) l++;
+    return l;
+}
+
+struct LayoutPlan {
+    BucketGeom g;
+    uint32_t stride;     // speculative bucket stride (items)
+    uint32_t cap_items;  // per-CTA item capacity of k_bucket_layout
+    size_t smem;
+    int threads;
+};
+
+// Bucket geometry for `n_expect` items over 2^q quotients: about 12k items
+// per bucket (one CTA sorts a bucket in shared memory), at most 4096 buckets
+// (the scatter keeps two u32 per bucket in shared memory).
+static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_t n_b_expect)
+{
+    const DeviceInfo &di = device_info(current_device());
+    LayoutPlan p;
+    uint32_t tb_lo = std::max<uint32_t>(7, q > 12 ? q - 12 : 0);
+    uint32_t tb_hi = std::min<uint32_t>(q, 15);
+    uint64_t denom = n_expect ? n_expect : 1;
+    uint32_t tb = ceil_log2((12000ull << q) / denom);
+    tb = std::min(std::max(tb, tb_lo), tb_hi);
+    p.g.q = q;
+    p.g.r = r;
+    p.g.tb = tb;
+    p.g.nb = 1u << (q - tb);
+    p.g.shift = r + tb;
+    p.g.fp_mask = (q + r >= 32) ? 0xFFFFFFFFu : ((1u << (q + r)) - 1u);
+    double avg_b = (double)n_b_expect / p.g.nb;
+    p.stride = (uint32_t)align_up((size_t)(avg_b + 10.0 * std::sqrt(avg_b) + 64.0), 32);
+    int bpe = (r + 3) / 8;
+    double avg = (double)n_expect / p.g.nb;
+    uint32_t need = (uint32_t)(avg * 1.05 + 10.0 * std::sqrt(avg) + 256.0);
+    p.threads = (1u << tb) >= 1024 ? 512 : 64;
+    size_t fixed = layout_smem_bytes(tb, 0, bpe);
+    size_t budget = 100 * 1024;
+    size_t maxsm = (size_t)(di.smem_optin > 0 ? di.smem_optin : 99 * 1024) - 4096;
+    if (fixed + (size_t)need * bpe > budget) budget = maxsm;
+    size_t cap = budget > fixed ? (budget - fixed) / bpe : 0;
+    cap = std::min<size_t>(cap & ~(size_t)15, 65520);
+    p.cap_items = (uint32_t)cap;
+    p.smem = layout_smem_bytes(tb, p.cap_items, bpe);
+    return p;
+}
+
+static size_t scatter_smem(uint32_t nb, bool pairs)
+{
+    size_t chunk = (size_t)SCATTER_THREADS * SCATTER_IPT;
+    return (pairs ? 2 : 1) * chunk * 4 + (size_t)nb * 8;
+}
+
+template <typename K>
+static cudaError_t set_smem(K kernel, size_t bytes)
+{
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// Device-side exclusive scan of bucket counts into bases (nb <= 4096).
+__global__ void __launch_bounds__(1024) k_scan_bases(const uint32_t *cnt, uint32_t nb, uint32_t *base)
+{
+    __shared__ uint32_t s[4097];
+    __shared__ uint32_t sw[33];
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) s[i] = cnt[i];
+    __syncthreads();
+    block_exclusive_scan_u32<1024>(s, nb, sw);
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) base[i] = s[i];
+}
+
+// ------------------------------------------------------------ the pipeline
+// Scratch for one rebuild: control words, look-back descriptors, fix-ups,
+// the bucketed batch (B) and optionally the table's extracted contents (A).
+struct Scratch {
+    uint32_t *bcnt;              // nb  : batch items per bucket
+    unsigned long long *status;  // nb  : look-back descriptors
+    uint32_t *ticket;
+    uint32_t *fix_cnt;
+    uint32_t *bbase;  // nb+1: exact batch bases
+    uint32_t *fix_list;
+    uint32_t fix_cap;
+    uint32_t *bitems;  // batch fingerprints
+    uint32_t *bidx;    // batch indices (sorted lookups)
+    // extracted table contents
+    Counts3 *tiles;
+    uint32_t *Q, *E, *abase, *acnt;
+    uint32_t *E2, *a2base, *a2cnt;
+    size_t ctrl_bytes;
+};
+
+struct ScratchReq {
+    uint32_t nb;
+    size_t batch_items;  // capacity of the bucketed batch
+    bool pairs;
+    bool extract;   // table contents needed
+    bool extract2;  // second table (merge)
+    uint32_t nslots;
+};
+
+static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *bytes_out)
+{
+    Scratch s{};
+    auto lay = [&](auto &c) {
+        size_t nb = r.nb;
+        s.bcnt = c.template take<uint32_t>(nb, 8);
+        s.status = c.template take<unsigned long long>(nb, 8);
+        s.ticket = c.template take<uint32_t>(1, 4);
+        s.fix_cnt = c.template take<uint32_t>(1, 4);
+        s.ctrl_bytes = c.off;
+        s.bbase = c.template take<uint32_t>(nb + 1);
+        s.fix_cap = std::max<uint32_t>(65536u, r.nslots / 8);
+        s.fix_list = c.template take<uint32_t>(s.fix_cap);
+        s.bitems = c.template take<uint32_t>(std::max<size_t>(r.batch_items, 1));
+        s.bidx = r.pairs ? c.template take<uint32_t>(std::max<size_t>(r.batch_items, 1)) : nullptr;
+        if (r.extract) {
+            size_t ntiles = (r.nslots + EXTRACT_TILE - 1) / EXTRACT_TILE;
+            s.tiles = c.template take<Counts3>(ntiles + 1);
+            s.Q = c.template take<uint32_t>(r.nslots);
+            s.E = c.template take<uint32_t>(r.nslots);
+            s.abase = c.template take<uint32_t>(nb + 1);
+            s.acnt = c.template take<uint32_t>(nb);
+            if (r.extract2) {
+                s.E2 = c.template take<uint32_t>(r.nslots);
+                s.a2base = c.template take<uint32_t>(nb + 1);
+                s.a2cnt = c.template take<uint32_t>(nb);
+            }
+        }
+    };
+    if (sizing_only) {
+        Sizer z;
+        lay(z);
+        *bytes_out = z.off;
+    } else {
+        Carver c(base);
+        lay(c);
+        *bytes_out = c.off;
+    }
+    return s;
+}
+
+// Extract a table's fingerprints (sorted for canonical tables) into E and
+// bucket them by quotient range.  Count of elements stays on the device.
+template <int BPE>
+static int extract_into(const uint8_t *table, uint32_t nslots, uint32_t r, const BucketGeom &g, Counts3 *tiles,
+                        uint32_t *Q, uint32_t *E, uint32_t *base, uint32_t *cnt, cudaStream_t s)
+{
+    uint32_t ntiles = (nslots + EXTRACT_TILE - 1) / EXTRACT_TILE;
+    count_launches(6);
+    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, tiles);
+    k_scan_counts3<<<1, 1024, 0, s>>>(tiles, ntiles);
+    k_occ_list<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, tiles, Q);
+    k_extract<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, r, tiles, Q, E);
+    uint32_t grid = (g.nb + 1 + 255) / 256;
+    k_sorted_bounds<<<grid, 256, 0, s>>>(E, &tiles[ntiles].ne, g.nb, g.shift, base, cnt);
+    k_bounds_to_counts<<<grid, 256, 0, s>>>(base, g.nb, cnt);
+    GQF_CK(cudaGetLastError());
+    return GQF_OK;
+}
+
+// Hash + bucket the batch keys.  exact: histogram + device scan first.
+static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, Scratch &sc, bool exact, bool pairs,
+                        uint32_t *err, cudaStream_t s)
+{
+    if (n == 0) return GQF_OK;
+    const uint32_t chunk = SCATTER_THREADS * SCATTER_IPT;
+    const uint32_t grid = (n + chunk - 1) / chunk;
+    const size_t sm = scatter_smem(p.g.nb, pairs);
+    if (exact) {
+        GQF_CK(set_smem(k_bucket_hist<SCATTER_THREADS, SCATTER_IPT>, p.g.nb * 4));
+        count_launches(2);
+        k_bucket_hist<SCATTER_THREADS, SCATTER_IPT><<<grid, SCATTER_THREADS, p.g.nb * 4, s>>>(keys, n, p.g, sc.bcnt);
+        k_scan_bases<<<1, 1024, 0, s>>>(sc.bcnt, p.g.nb, sc.bbase);
+        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, p.g.nb * 4, s));
+    }
+    count_launches(1);
+    if (pairs) {
+        auto kfn = k_hash_bucket<SCATTER_THREADS, SCATTER_IPT, true>;
+        GQF_CK(set_smem(kfn, sm));
+        kfn<<<grid, SCATTER_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
+                                              sc.bcnt, sc.bitems, sc.bidx, err);
+    } else {
+        auto kfn = k_hash_bucket<SCATTER_THREADS, SCATTER_IPT, false>;
+        GQF_CK(set_smem(kfn, sm));
+        kfn<<<grid, SCATTER_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
+                                              sc.bcnt, sc.bitems, nullptr, err);
+    }
+    GQF_CK(cudaGetLastError());
+    return GQF_OK;
+}
+
+template <int BPE>
+static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table, const BucketSrc &A,
+                         const BucketSrc &B, int op, int nodup, Scratch &sc, uint32_t *err, cudaStream_t s)
+{
+    // slots past the last bucket's quotients only receive spill: clear them
+    size_t tail = (size_t)(1u << tg.q) * BPE;
+    if (tg.T > tail) GQF_CK(cudaMemsetAsync(table + tail, 0, tg.T - tail, s));
+    LayoutArgs a;
+    a.A = A;
+    a.B = B;
+    a.table = table;
+    a.q = tg.q;
+    a.r = tg.r;
+    a.tb = p.g.tb;
+    a.nb = p.g.nb;
+    a.nslots = tg.nslots;
+    a.cap_items = p.cap_items;
+    a.op = op;
+    a.nodup = nodup;
+    a.status = sc.status;
+    a.ticket = sc.ticket;
+    a.fix_list = sc.fix_list;
+    a.fix_cnt = sc.fix_cnt;
+    a.fix_cap = sc.fix_cap;
+    a.err = err;
+    if (p.threads == 512) {
+        auto k = k_bucket_layout<512, BPE>;
+        GQF_CK(set_smem(k, p.smem));
+        k<<<p.g.nb, 512, p.smem, s>>>(a);
+    } else {
+        auto k = k_bucket_layout<64, BPE>;
+        GQF_CK(set_smem(k, p.smem));
+        k<<<p.g.nb, 64, p.smem, s>>>(a);
+    }
+    const DeviceInfo &di = device_info(current_device());
+    count_launches(2);
+    k_fixup_occ<BPE><<<di.sms * 2, 256, 0, s>>>(table, sc.fix_list, sc.fix_cnt, sc.fix_cap);
+    GQF_CK(cudaGetLastError());
+    return GQF_OK;
+}
+
+enum class Src { NONE, TABLE, KEYS, TABLE2 };
+
+// One rebuild: A = current contents of `table` (when the op needs them) or
+// of `table2`, B = hashed batch keys (or the second table's contents).
+template <int BPE>
+static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, uint32_t n, int op, int nodup,
+                   cudaStream_t s, float *ms)
+{
+    const SqfGeom tg = geom_of(qf);
+    const bool needA = op != OP_BUILD;
+    const bool bFromTable = qf2 != nullptr;
+    uint64_t nA = needA ? tg.nslots : 0;  // worst case for sizing
+    uint64_t nB = bFromTable ? tg.nslots : n;
+    // expected items: the table holds at most nslots
+    uint64_t expect = std::min<uint64_t>((needA ? (uint64_t)(tg.nslots * 0.9) : 0) + (bFromTable ? (uint64_t)(tg.nslots * 0.9) : n),
+                                         (uint64_t)tg.nslots * 2);
+    LayoutPlan p = plan_layout(tg.q, tg.r, expect, bFromTable ? 0 : n);
+    ScratchReq req{p.g.nb, bFromTable ? 0 : (size_t)p.g.nb * p.stride, false, needA, bFromTable, tg.nslots};
+    (void)nA;
+    (void)nB;
+    int dev = current_device();
+    Arena &ar = arena(dev);
+    std::lock_guard<std::mutex> lk(ar.mu);
+    size_t bytes = 0;
+    carve(nullptr, req, true, &bytes);
+    // exact-mode batch needs n items at most
+    size_t bytes_exact = 0;
+    ScratchReq req_exact = req;
+    req_exact.batch_items = std::max<size_t>(n, 1);
+    carve(nullptr, req_exact, true, &bytes_exact);
+    void *base = arena_reserve(ar, std::max(bytes, bytes_exact));
+    if (!base) return GQF_ERR_NOMEM;
+    // A timed build uses speculative bucket strides (one pass over the keys)
+    // and reruns with exact bucket bases if a bucket overflowed; the rerun
+    // rewrites the whole table from the keys.  Updates read the table, so
+    // they and all asynchronous calls bucket exactly.
+    bool exact = !(op == OP_BUILD && ms != nullptr);
+    for (int attempt = 0; attempt < 2; attempt++) {
+        Scratch sc = carve(base, exact ? req_exact : req, false, &bytes);
+        int st = call_begin(ar, s, ms != nullptr);
+        if (st) return st;
+        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
+        GQF_CK(cudaMemsetAsync(sc.fix_cnt, 0, 4, s));
+        BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
+        if (needA) {
+            st = extract_into<BPE>(qf->table, tg.nslots, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt, s);
+            if (st) return st;
+            A = BucketSrc{sc.E, sc.abase, 0, sc.acnt};
+        }
+        if (bFromTable) {
+            st = extract_into<BPE>(qf2->table, tg.nslots, tg.r, p.g, sc.tiles, sc.Q, sc.E2, sc.a2base, sc.a2cnt, s);
+            if (st) return st;
+            B = BucketSrc{sc.E2, sc.a2base, 0, sc.a2cnt};
+        } else if (n) {
+            st = bucket_batch(keys, n, p, sc, exact, false, ar.err, s);
+            if (st) return st;
+            B = exact ? BucketSrc{sc.bitems, sc.bbase, 0, sc.bcnt} : BucketSrc{sc.bitems, nullptr, p.stride, sc.bcnt};
+        }
+        st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, sc, ar.err, s);
+        if (st) return st;
+        if (!ms) return call_end(ar, s, nullptr);
+        // synchronous: look at the error word before deciding
+        GQF_CK(cudaEventRecord(ar.ev1, s));
+        GQF_CK(cudaEventSynchronize(ar.ev1));
+        uint32_t e = 0;
+        GQF_CK(cudaMemcpy(&e, ar.err, 4, cudaMemcpyDeviceToHost));
+        if ((e & DEV_ERR_BUCKET_OVER) && !exact) {
+            exact = true;
+            continue;
+        }
+        GQF_CK(cudaEventElapsedTime(ms, ar.ev0, ar.ev1));
+        return dev_err_to_status(e);
+    }
+    return GQF_ERR_FULL;
+}
+
+template <int BPE>
+static int lookup_unsorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint32_t *out, cudaStream_t s, float *ms)
+{
+    const SqfGeom tg = geom_of(qf);
+    Arena &ar = arena(current_device());
+    std::lock_guard<std::mutex> lk(ar.mu);
+    int st = call_begin(ar, s, ms != nullptr);
+    if (st) return st;
+    TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
+    if (n > 0) {
+        const DeviceInfo &di = device_info(current_device());
+        uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)di.sms * 64);
+        k_lookup_unsorted<BPE><<<grid, 256, 0, s>>>(keys, (uint32_t)n, v, out);
+        count_launches(1);
+    }
+    return call_end(ar, s, ms);
+}
+
+template <int BPE>
+static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint32_t *out, cudaStream_t s, float *ms)
+{
+    const SqfGeom tg = geom_of(qf);
+    LayoutPlan p = plan_layout(tg.q, tg.r, (uint64_t)tg.nslots * 8 / 10, (uint64_t)n);
+    // query buckets: aim for ~4k queries per bucket, table-aligned
+    ScratchReq req{p.g.nb, (size_t)std::max(n, 1), true, false, false, tg.nslots};
+    Arena &ar = arena(current_device());
+    std::lock_guard<std::mutex> lk(ar.mu);
+    size_t bytes = 0;
+    carve(nullptr, req, true, &bytes);
+    void *base = arena_reserve(ar, bytes);
+    if (!base) return GQF_ERR_NOMEM;
+    Scratch sc = carve(base, req, false, &bytes);
+    int st = call_begin(ar, s, ms != nullptr);
+    if (st) return st;
+    if (n > 0) {
+        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
+        st = bucket_batch(keys, (uint32_t)n, p, sc, true, true, ar.err, s);
+        if (st) return st;
+        TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
+        BucketSrc src{sc.bitems, sc.bbase, 0, sc.bcnt};
+        k_lookup_bucketed<BPE><<<p.g.nb, 256, 0, s>>>(src, sc.bidx, v, out);
+        count_launches(1);
+    }
+    return call_end(ar, s, ms);
+}
+
+}  // namespace gqf
+
+using namespace gqf;
+
+#define BPE_DISPATCH(qf, fn, ...) (((qf)->rbits + 3) / 8 == 1 ? fn<1>(__VA_ARGS__) : fn<2>(__VA_ARGS__))
+
+extern "C" {
+
+size_t gqf_sqf_table_bytes(unsigned int q, unsigned int r)
+{
+    // calcNumSlotsGPU, quotientFilter.cu:37-42
+    size_t table_bits = (size_t)(1u << q) * (r + 3);
+    size_t table_slots = table_bits / 8;
+    return (size_t)((double)table_slots * 1.1);
+}
+
+unsigned int gqf_sqf_num_slots(unsigned int q) { return (unsigned int)((double)(1u << q) * 1.1); }
+
+int gqf_sqf_init(gqf_sqf *qf, unsigned int q, unsigned int r)
+{
+    if (!qf || !qr_ok(q, r)) return GQF_ERR_ARG;
+    qf->qbits = q;
+    qf->rbits = r;
+    qf->bytesPerElement = (r + 3) / 8;
+    size_t T = gqf_sqf_table_bytes(q, r);
+    unsigned char *t = nullptr;
+    GQF_CK(cudaMalloc(&t, align_up(T, 256)));
+    GQF_CK(cudaMemset(t, 0, align_up(T, 256)));
+    qf->table = t;
+    return GQF_OK;
+}
+
+int gqf_sqf_free(gqf_sqf *qf)
+{
+    if (!qf) return GQF_ERR_ARG;
+    if (qf->table) GQF_CK(cudaFree(qf->table));
+    qf->table = nullptr;
+    return GQF_OK;
+}
+
+static bool sqf_ok(const gqf_sqf *qf) { return qf && qf->table && qr_ok(qf->qbits, qf->rbits); }
+
+int gqf_sqf_bulk_build(const gqf_sqf *qf, int n, const uint32_t *d_keys, int no_duplicates, void *stream, float *ms)
+{
+    if (!sqf_ok(qf) || n < 0 || (n > 0 && !d_keys)) return GQF_ERR_ARG;
+    return BPE_DISPATCH(qf, rebuild, qf, nullptr, d_keys, (uint32_t)n, OP_BUILD, no_duplicates ? 1 : 0,
+                        static_cast<cudaStream_t>(stream), ms);
+}
+
+int gqf_sqf_insert(const gqf_sqf *qf, int n, const uint32_t *d_keys, void *stream, float *ms)
+{
+    if (!sqf_ok(qf) || n < 0 || (n > 0 && !d_keys)) return GQF_ERR_ARG;
+    return BPE_DISPATCH(qf, rebuild, qf, nullptr, d_keys, (uint32_t)n, OP_INSERT, 1, static_cast<cudaStream_t>(stream),
+                        ms);
+}
+
+int gqf_sqf_delete(const gqf_sqf *qf, int n, const uint32_t *d_keys, void *stream, float *ms)
+{
+    if (!sqf_ok(qf) || n < 0 || (n > 0 && !d_keys)) return GQF_ERR_ARG;
+    return BPE_DISPATCH(qf, rebuild, qf, nullptr, d_keys, (uint32_t)n, OP_DELETE, 0, static_cast<cudaStream_t>(stream),
+                        ms);
+}
+
+int gqf_sqf_insert_via_merge(const gqf_sqf *qf, const uint32_t *d_old, int n_old, const uint32_t *d_new, int n_new,
+                             int no_duplicates, void *stream, float *ms)
+{
+    (void)d_old;
+    (void)n_old;
+    if (!sqf_ok(qf) || n_new < 0 || (n_new > 0 && !d_new)) return GQF_ERR_ARG;
+    return BPE_DISPATCH(qf, rebuild, qf, nullptr, d_new, (uint32_t)n_new, OP_MERGE, no_duplicates ? 1 : 0,
+                        static_cast<cudaStream_t>(stream), ms);
+}
+
+int gqf_sqf_merge(const gqf_sqf *qf1, const gqf_sqf *qf2, int no_duplicates, void *stream, float *ms)
+{
+    if (!sqf_ok(qf1) || !sqf_ok(qf2)) return GQF_ERR_ARG;
+    if (qf1->qbits != qf2->qbits || qf1->rbits != qf2->rbits) return GQF_ERR_MISMATCH;
+    return BPE_DISPATCH(qf1, rebuild, qf1, qf2, nullptr, 0u, OP_MERGE, no_duplicates ? 1 : 0,
+                        static_cast<cudaStream_t>(stream), ms);
+}
+
+int gqf_sqf_lookup_unsorted(const gqf_sqf *qf, int n, const uint32_t *d_keys, uint32_t *d_out, void *stream, float *ms)
+{
+    if (!sqf_ok(qf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
+    return BPE_DISPATCH(qf, lookup_unsorted_t, qf, n, d_keys, d_out, static_cast<cudaStream_t>(stream), ms);
+}
+
+int gqf_sqf_lookup_sorted(const gqf_sqf *qf, int n, const uint32_t *d_keys, uint32_t *d_out, void *stream, float *ms)
+{
+    if (!sqf_ok(qf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
+    return BPE_DISPATCH(qf, lookup_sorted_t, qf, n, d_keys, d_out, static_cast<cudaStream_t>(stream), ms);
+}
+
+}  // extern "C"

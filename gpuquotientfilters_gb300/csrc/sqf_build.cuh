@@ -1,0 +1,569 @@
+// SQF bulk build: hash -> quotient-range buckets -> per-bucket layout.
+//
+// The reference (quotientFilter.cu:1446-1559) hashes, radix-sorts all
+// fingerprints with Thrust, then iterates a host-driven fixpoint over
+// 2^q/q segments until no segment overflows (:1516-1530), and finally
+// scatters elements and read-modify-writes occupied bits.  Its result is a
+// pure function of the sorted fingerprint multiset: item i of the sorted
+// order lands at slot pos_i = max(quotient_i, pos_{i-1} + 1).  This build
+// computes that layout directly:
+//
+//   k_hash_bucket   one pass over the keys: Normal_APHash, then a
+//                   CTA-local counting sort by bucket (bucket = the top
+//                   q - tb quotient bits) and coalesced runs into per-bucket
+//                   regions (one global atomic per CTA and bucket).
+//   k_bucket_layout one CTA per bucket (2^tb quotients): counting sort by
+//                   quotient in shared memory, tiny per-quotient remainder
+//                   sorts, then the slot recurrence as a block scan of
+//                   c -> max(c + n, F) maps, chained across buckets with a
+//                   decoupled look-back; every slot of the bucket's write
+//                   range is produced in shared memory and stored once with
+//                   16-byte stores (no read-modify-write of the table).
+//   k_fixup_occ     occupied bits of quotients whose slot was written by an
+//                   earlier bucket (the spill of a cluster that crosses a
+//                   bucket boundary).
+#pragma once
+
+#include "qf_device.cuh"
+
+namespace gqf {
+
+struct BucketGeom {
+    uint32_t q, r, tb, nb;  // S = 1 << tb quotients per bucket, nb = 2^(q - tb)
+    uint32_t shift;         // r + tb: bucket index = fp >> shift
+    uint32_t fp_mask;       // (1 << (q + r)) - 1
+};
+
+constexpr int SCATTER_THREADS = 512;
+constexpr int SCATTER_IPT = 32;  // 16K keys per CTA
+constexpr int LAYOUT_THREADS = 512;
+constexpr uint32_t SPILL_SLOTS = 4096;  // tile buffer headroom past the bucket
+constexpr uint32_t SPIN_LIMIT = 1u << 22;
+
+// Exclusive scan of `cnt` (nvals entries of u32 in shared memory) in place,
+// by a block of THREADS threads; returns the total.  Each thread owns a
+// contiguous run of ceil(nvals / THREADS) entries.
+template <int THREADS>
+__device__ uint32_t block_exclusive_scan_u32(uint32_t *cnt, uint32_t nvals, uint32_t *s_warp)
+{
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t per = (nvals + THREADS - 1) / THREADS;
+    const uint32_t beg = min(nvals, tid * per), end = min(nvals, beg + per);
+    uint32_t sum = 0;
+    for (uint32_t i = beg; i < end; i++) sum += cnt[i];
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t v = lane < THREADS / 32 ? s_warp[lane] : 0;
+        uint32_t iv = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, iv, o);
+            if (lane >= o) iv += t;
+        }
+        if (lane < THREADS / 32) s_warp[lane] = iv - v;  // exclusive warp offsets
+        if (lane == THREADS / 32 - 1) s_warp[32] = iv;   // total
+    }
+    __syncthreads();
+    uint32_t run = s_warp[wid] + incl - sum;
+    for (uint32_t i = beg; i < end; i++) {
+        uint32_t c = cnt[i];
+        cnt[i] = run;
+        run += c;
+    }
+    uint32_t total = s_warp[32];
+    __syncthreads();
+    return total;
+}
+
+// ---------------------------------------------------------------------
+// K1: hash + bucket scatter.  out[base(b) + j] holds the j-th fingerprint
+// of bucket b (order within a bucket is arbitrary).  base(b) = b * cap in
+// speculative mode (bucket_base == nullptr); a bucket that would exceed cap
+// sets DEV_ERR_BUCKET_OVER and the host reruns with exact bases.
+// Dynamic smem: items[THREADS*IPT] + cursor[nb] + gbase[nb] (u32).
+// With `vals` non-null the kernel scatters (fingerprint, index) pairs: the
+// pair payload is the key's position in the input (sorted lookups).
+// ---------------------------------------------------------------------
+template <int THREADS, int IPT, bool PAIRS>
+__global__ void __launch_bounds__(THREADS) k_hash_bucket(
+    const uint32_t *__restrict__ keys, uint32_t n, BucketGeom g,
+    const uint32_t *__restrict__ bucket_base, uint32_t cap,
+    uint32_t *__restrict__ bucket_cnt, uint32_t *__restrict__ out,
+    uint32_t *__restrict__ out_idx, uint32_t *__restrict__ err)
+{
+    extern __shared__ __align__(16) uint32_t smem_scatter[];
+    constexpr uint32_t CHUNK = THREADS * IPT;
+    uint32_t *s_items = smem_scatter;
+    uint32_t *s_idx = s_items + CHUNK;  // only when PAIRS
+    uint32_t *s_cur = s_items + (PAIRS ? 2 * CHUNK : CHUNK);
+    uint32_t *s_gb = s_cur + g.nb;
+    __shared__ uint32_t s_warp[33];
+    const int tid = threadIdx.x;
+    const uint64_t c0 = (uint64_t)blockIdx.x * CHUNK;
+    const uint32_t cnt = (uint32_t)min((uint64_t)CHUNK, (uint64_t)n - c0);
+
+    for (uint32_t i = tid; i < g.nb; i += THREADS) s_cur[i] = 0;
+    __syncthreads();
+
+    uint32_t fp[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        uint32_t j = k * THREADS + tid;
+        fp[k] = 0xFFFFFFFFu;
+        if (j < cnt) {
+            fp[k] = aphash32(__ldg(keys + c0 + j)) & g.fp_mask;
+            atomicAdd(&s_cur[fp[k] >> g.shift], 1u);
+        }
+    }
+    __syncthreads();
+    // exclusive offsets + one global reservation per non-empty bucket
+    {
+        const uint32_t per = (g.nb + THREADS - 1) / THREADS;
+        const uint32_t beg = min(g.nb, tid * per), end = min(g.nb, beg + per);
+        for (uint32_t b = beg; b < end; b++) {
+            uint32_t c = s_cur[b];
+            s_gb[b] = c ? atomicAdd(bucket_cnt + b, c) : 0u;
+        }
+    }
+    block_exclusive_scan_u32<THREADS>(s_cur, g.nb, s_warp);
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        uint32_t j = k * THREADS + tid;
+        if (j < cnt) {
+            uint32_t p = atomicAdd(&s_cur[fp[k] >> g.shift], 1u);
+            s_items[p] = fp[k];
+            if (PAIRS) s_idx[p] = (uint32_t)(c0 + j);
+        }
+    }
+    __syncthreads();
+    // s_cur[b] is now the end of bucket b's run in s_items
+    for (uint32_t i = tid; i < cnt; i += THREADS) {
+        uint32_t v = s_items[i];
+        uint32_t b = v >> g.shift;
+        uint32_t start = b ? s_cur[b - 1] : 0u;
+        uint32_t gpos = s_gb[b] + (i - start);
+        if (gpos < cap) {
+            size_t dst = (bucket_base ? (size_t)bucket_base[b] : (size_t)b * cap) + gpos;
+            out[dst] = v;
+            if (PAIRS) out_idx[dst] = s_idx[i];
+        } else {
+            atomicOr(err, DEV_ERR_BUCKET_OVER);
+        }
+    }
+}
+
+// Histogram-only pass for exact bucket bases (used when a speculative
+// bucket overflowed).
+template <int THREADS, int IPT>
+__global__ void __launch_bounds__(THREADS) k_bucket_hist(
+    const uint32_t *__restrict__ keys, uint32_t n, BucketGeom g, uint32_t *__restrict__ bucket_cnt)
+{
+    extern __shared__ __align__(16) uint32_t smem_hist[];
+    constexpr uint32_t CHUNK = THREADS * IPT;
+    const uint64_t c0 = (uint64_t)blockIdx.x * CHUNK;
+    const uint32_t cnt = (uint32_t)min((uint64_t)CHUNK, (uint64_t)n - c0);
+    for (uint32_t i = threadIdx.x; i < g.nb; i += THREADS) smem_hist[i] = 0;
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < cnt; j += THREADS) {
+        uint32_t fp = aphash32(__ldg(keys + c0 + j)) & g.fp_mask;
+        atomicAdd(&smem_hist[fp >> g.shift], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < g.nb; b += THREADS)
+        if (smem_hist[b]) atomicAdd(bucket_cnt + b, smem_hist[b]);
+}
+
+// ---------------------------------------------------------------------
+// Look-back over bucket descriptors (single thread).  Returns the slot at
+// which bucket b's items start being laid out (c_in).
+// ---------------------------------------------------------------------
+__device__ inline uint32_t lookback_cin(unsigned long long *status, uint32_t b, uint32_t *err)
+{
+    LayoutFn acc{0u, 0u};
+    for (int j = (int)b - 1; j >= 0; j--) {
+        unsigned long long v;
+        uint32_t spins = 0;
+        for (;;) {
+            v = ld_acquire_u64(status + j);
+            if (v >> 62) break;
+            if (++spins > SPIN_LIMIT) {
+                atomicOr(err, DEV_ERR_TIMEOUT);
+                return acc.apply(0u);
+            }
+            __nanosleep(64);
+        }
+        if ((v >> 62) == 2ull) return acc.apply((uint32_t)(v & LB_VMAX));
+        LayoutFn f{(uint32_t)((v >> 31) & LB_VMAX), (uint32_t)(v & LB_VMAX)};
+        acc = compose(f, acc);
+    }
+    return acc.apply(0u);
+}
+
+// u16 counters packed two per u32 word
+__device__ __forceinline__ uint32_t cnt16_get(const uint32_t *a, uint32_t i)
+{
+    return (a[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+}
+__device__ __forceinline__ uint32_t cnt16_fetch_inc(uint32_t *a, uint32_t i)
+{
+    uint32_t old = atomicAdd(a + (i >> 1), 1u << ((i & 1) * 16));
+    return (old >> ((i & 1) * 16)) & 0xFFFFu;
+}
+
+template <typename T>
+__device__ void small_sort(T *v, uint32_t n)
+{
+    if (n < 2) return;
+    if (n <= 24) {
+        for (uint32_t i = 1; i < n; i++) {
+            T x = v[i];
+            int j = (int)i - 1;
+            while (j >= 0 && v[j] > x) {
+                v[j + 1] = v[j];
+                j--;
+            }
+            v[j + 1] = x;
+        }
+        return;
+    }
+    // heap sort for the rare large group (skewed input)
+    auto sift = [&](uint32_t root, uint32_t end) {
+        while (2 * root + 1 < end) {
+            uint32_t c = 2 * root + 1;
+            if (c + 1 < end && v[c] < v[c + 1]) c++;
+            if (!(v[root] < v[c])) return;
+            T t = v[root];
+            v[root] = v[c];
+            v[c] = t;
+            root = c;
+        }
+    };
+    for (int s = (int)n / 2 - 1; s >= 0; s--) sift((uint32_t)s, n);
+    for (uint32_t e = n - 1; e > 0; e--) {
+        T t = v[0];
+        v[0] = v[e];
+        v[e] = t;
+        sift(0, e);
+    }
+}
+
+// Per remainder value, how many copies the rebuilt group keeps, given ca
+// copies from source A (the table's current contents) and cb from source B
+// (the batch).  The reference semantics each op reproduces:
+//   OP_BUILD   bulkBuildSegmentedLayouts: all of B, unique when NoDuplicates
+//              (quotientFilter.cu:1478-1482)
+//   OP_INSERT  insert: a fingerprint already present is left alone, a new one
+//              is stored once (insertItemGPU :499-504)
+//   OP_DELETE  superclusterDeletes: each delete removes one stored copy
+//              (deleteItemGPU :1076-1200)
+//   OP_MERGE   insertViaMerge / mergeTwoFilters: merged multiset, unique when
+//              NoDuplicates (:1659-1664, :1808-1813)
+enum LayoutOp : int { OP_BUILD = 0, OP_INSERT = 1, OP_DELETE = 2, OP_MERGE = 3 };
+
+__device__ __forceinline__ uint32_t keep_count(int op, int nodup, uint32_t ca, uint32_t cb)
+{
+    switch (op) {
+    case OP_INSERT: return ca ? ca : (cb ? 1u : 0u);
+    case OP_DELETE: return ca > cb ? ca - cb : 0u;
+    default: return nodup ? ((ca + cb) ? 1u : 0u) : ca + cb;
+    }
+}
+
+// One source of fingerprints per bucket: items[base(b) .. base(b)+cnt[b]).
+struct BucketSrc {
+    const uint32_t *items;
+    const uint32_t *base;  // nullptr: b * stride
+    uint32_t stride;
+    const uint32_t *cnt;   // nullptr: source absent
+    __device__ __forceinline__ size_t start(uint32_t b) const { return base ? (size_t)base[b] : (size_t)b * stride; }
+    __device__ __forceinline__ uint32_t count(uint32_t b) const { return cnt ? cnt[b] : 0u; }
+};
+
+struct LayoutArgs {
+    BucketSrc A, B;
+    uint8_t *table;
+    uint32_t q, r, tb, nb, nslots;
+    uint32_t cap_items;  // tagged remainders one CTA can hold
+    int op, nodup;
+    unsigned long long *status;
+    uint32_t *ticket;
+    uint32_t *fix_list;
+    uint32_t *fix_cnt;
+    uint32_t fix_cap;
+    uint32_t *err;
+};
+
+// Shared-memory bytes of k_bucket_layout for a geometry.
+__host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_items, int bpe)
+{
+    size_t S = (size_t)1 << tb;
+    size_t cnt = S * 2 + 16;  // packed u16 counters (+ spare words)
+    size_t rem = ((size_t)cap_items * bpe + 15) & ~(size_t)15;
+    size_t tile = (S + SPILL_SLOTS) * bpe + 32;
+    return cnt + rem + tile;
+}
+
+// Walks the groups of quotients [qb, qb+QPT) in slot order and calls
+// emit(xa, rem, k) for every item the rebuilt table holds (k = index of the
+// item within its quotient's run).  Groups hold (rem << 1 | source) sorted.
+template <typename Rem, typename Emit>
+__device__ __forceinline__ void walk_groups(const uint32_t *s_cnt, const Rem *s_rem, uint32_t qb, uint32_t QPT,
+                                            uint32_t x0, int op, int nodup, Emit &&emit)
+{
+    for (uint32_t j = 0; j < QPT; j++) {
+        uint32_t x = qb + j;
+        uint32_t g0 = x ? cnt16_get(s_cnt, x - 1) : 0u, g1 = cnt16_get(s_cnt, x);
+        uint32_t kk = 0;
+        for (uint32_t k = g0; k < g1;) {
+            uint32_t v = (uint32_t)s_rem[k] >> 1, ca = 0, cb = 0;
+            while (k < g1 && ((uint32_t)s_rem[k] >> 1) == v) {
+                if (s_rem[k] & 1) cb++; else ca++;
+                k++;
+            }
+            uint32_t keep = keep_count(op, nodup, ca, cb);
+            for (uint32_t c = 0; c < keep; c++) emit(x0 + x, v, kk++);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// K2: one CTA per bucket (taken in ticket order for the look-back).
+// ---------------------------------------------------------------------
+template <int THREADS, int BPE>
+__global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
+{
+    using Rem = typename std::conditional<BPE == 1, uint8_t, uint16_t>::type;
+    extern __shared__ __align__(16) uint8_t smem_layout[];
+    const uint32_t S = 1u << a.tb;
+    uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem_layout);  // S/2 + 4 words
+    Rem *s_rem = reinterpret_cast<Rem *>(smem_layout + (size_t)S * 2 + 16);
+    uint8_t *s_tile = smem_layout + (size_t)S * 2 + 16 +
+                      (((size_t)a.cap_items * BPE + 15) & ~(size_t)15);
+    const uint32_t BUF = S + SPILL_SLOTS;  // slots the tile buffer holds
+
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_b, s_cin, s_cout, s_nfix, s_fbase;
+    __shared__ LayoutFn s_wfn[THREADS / 32];
+    __shared__ LayoutFn s_wexcl[THREADS / 32];
+    __shared__ uint32_t s_fix[256];
+
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) {
+        s_b = atomicAdd(a.ticket, 1u);
+        s_nfix = 0;
+    }
+    __syncthreads();
+    const uint32_t b = s_b;
+    const uint32_t na = a.A.count(b), nbn = a.B.count(b);
+    const uint32_t n = na + nbn;
+    const size_t abase = na ? a.A.start(b) : 0, bbase = nbn ? a.B.start(b) : 0;
+    const uint32_t x0 = b * S;  // first quotient of the bucket
+    const uint32_t rmask = (1u << a.r) - 1u;
+
+    if (n > a.cap_items) {
+        // cannot sort here: flag it (the host falls back) and keep the chain alive
+        if (tid == 0) {
+            atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+            st_release_u64(a.status + b, lb_pack_inc(x0));
+        }
+        return;
+    }
+    auto item = [&](uint32_t i) -> uint32_t {
+        return i < na ? a.A.items[abase + i] : a.B.items[bbase + (i - na)];
+    };
+
+    // A: counting sort of tagged remainders by local quotient
+    for (uint32_t i = tid; i < S / 2 + 4; i += THREADS) s_cnt[i] = 0;
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += THREADS) cnt16_fetch_inc(s_cnt, (item(i) >> a.r) & (S - 1));
+    __syncthreads();
+    // exclusive scan of the u16 counters: thread owns QPT consecutive quotients
+    const uint32_t QPT = S / THREADS;  // S >= 2 * THREADS, power of two
+    const uint32_t qb = tid * QPT;
+    {
+        uint32_t sum = 0;
+        for (uint32_t j = 0; j < QPT; j++) sum += cnt16_get(s_cnt, qb + j);
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) s_warp[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t v = lane < THREADS / 32 ? s_warp[lane] : 0;
+            uint32_t iv = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, iv, o);
+                if (lane >= o) iv += t;
+            }
+            if (lane < THREADS / 32) s_warp[lane] = iv - v;
+        }
+        __syncthreads();
+        uint32_t run = s_warp[wid] + incl - sum;
+        for (uint32_t j = 0; j < QPT; j += 2) {  // QPT even: whole words
+            uint32_t c0 = cnt16_get(s_cnt, qb + j), c1 = cnt16_get(s_cnt, qb + j + 1);
+            s_cnt[(qb + j) >> 1] = run | ((run + c0) << 16);
+            run += c0 + c1;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += THREADS) {
+        uint32_t fp = item(i);
+        uint32_t p = cnt16_fetch_inc(s_cnt, (fp >> a.r) & (S - 1));
+        s_rem[p] = (Rem)(((fp & rmask) << 1) | (i >= na ? 1u : 0u));
+    }
+    __syncthreads();
+    // s_cnt[x] now holds the END of group x; group x = [end(x-1), end(x))
+
+    // B: sort each group; walk the recurrence once from slot 0
+    LayoutFn fn{0u, 0u};
+    {
+        for (uint32_t j = 0; j < QPT; j++) {
+            uint32_t x = qb + j;
+            uint32_t g0 = x ? cnt16_get(s_cnt, x - 1) : 0u, g1 = cnt16_get(s_cnt, x);
+            if (g1 - g0 > 1) small_sort(s_rem + g0, g1 - g0);
+        }
+        uint32_t c = 0, cnt_items = 0;
+        walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, [&](uint32_t xa, uint32_t, uint32_t) {
+            uint32_t pos = xa > c ? xa : c;
+            c = pos + 1;
+            cnt_items++;
+        });
+        fn.n = cnt_items;
+        fn.F = cnt_items ? c : 0u;
+    }
+    // C: block scan of layout maps (exclusive per thread + bucket total)
+    LayoutFn incl = fn;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        LayoutFn p;
+        p.n = __shfl_up_sync(0xffffffffu, incl.n, o);
+        p.F = __shfl_up_sync(0xffffffffu, incl.F, o);
+        if (lane >= o) incl = compose(p, incl);
+    }
+    LayoutFn wexcl;
+    wexcl.n = __shfl_up_sync(0xffffffffu, incl.n, 1);
+    wexcl.F = __shfl_up_sync(0xffffffffu, incl.F, 1);
+    if (lane == 0) wexcl = LayoutFn{0u, 0u};
+    if (lane == 31) s_wfn[wid] = incl;
+    __syncthreads();
+    if (tid == 0) {
+        LayoutFn acc{0u, 0u};
+        for (int w = 0; w < THREADS / 32; w++) {
+            s_wexcl[w] = acc;
+            acc = compose(acc, s_wfn[w]);
+        }
+        // D: publish, look back, publish inclusive
+        if (acc.n > LB_VMAX / 2 || acc.F > LB_VMAX / 2) atomicOr(a.err, DEV_ERR_FULL);
+        uint32_t cin;
+        if (b == 0) {
+            cin = 0;
+        } else {
+            st_release_u64(a.status + b, lb_pack_agg(acc.n, acc.F));
+            cin = lookback_cin(a.status, b, a.err);
+        }
+        uint32_t cout = acc.apply(cin);
+        st_release_u64(a.status + b, lb_pack_inc(cout));
+        s_cin = cin;
+        s_cout = cout;
+    }
+    __syncthreads();
+    const uint32_t cin = s_cin, cout = s_cout;
+    const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
+    const uint32_t lo = cin > x0 ? cin : x0;
+    uint32_t hi = cout > x0 + S ? cout : x0 + S;
+    if (hi > a.nslots) {
+        if (cout > a.nslots && tid == 0) atomicOr(a.err, DEV_ERR_FULL);
+        hi = a.nslots;
+    }
+    const uint32_t span = hi > lo ? hi - lo : 0u;
+    const uint32_t bufslots = span < BUF ? span : BUF;
+    const size_t gs = (size_t)lo * BPE;             // first table byte written
+    const size_t ge = gs + (size_t)bufslots * BPE;  // end of the buffered part
+    const size_t gal = gs & ~(size_t)15;            // smem byte 0 <-> table byte gal
+    for (size_t i = tid * 16; i < ge - gal; i += THREADS * 16)
+        *reinterpret_cast<uint4 *>(s_tile + i) = make_uint4(0, 0, 0, 0);
+    __syncthreads();
+
+    // E: emit elements
+    {
+        uint32_t c = texcl.apply(cin);
+        walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, [&](uint32_t xa, uint32_t rem, uint32_t kk) {
+            uint32_t pos = xa > c ? xa : c;
+            c = pos + 1;
+            if (pos >= hi) return;  // past the table: reported as FULL
+            uint32_t e = (rem << 3) | (kk ? 2u : 0u) | (pos != xa ? 1u : 0u);
+            uint8_t *d = (pos - lo < bufslots) ? s_tile + ((size_t)pos * BPE - gal) : a.table + (size_t)pos * BPE;
+            if (BPE == 1) {
+                d[0] = (uint8_t)e;
+            } else {
+                d[0] = (uint8_t)(e >> 8);
+                d[1] = (uint8_t)e;
+            }
+        });
+    }
+    __syncthreads();
+    // F: occupied bits (own tile) or fix-ups (slot written by an earlier
+    // bucket); a quotient is occupied iff the rebuilt group is non-empty
+    {
+        uint32_t last_x = 0xFFFFFFFFu;
+        walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, [&](uint32_t xa, uint32_t, uint32_t kk) {
+            if (kk != 0 || xa == last_x) return;
+            last_x = xa;
+            if (xa >= lo) {
+                s_tile[(size_t)xa * BPE + (BPE - 1) - gal] |= 4u;
+            } else {
+                uint32_t p = atomicAdd(&s_nfix, 1u);
+                if (p < 256) {
+                    s_fix[p] = xa;
+                } else {
+                    uint32_t gp = atomicAdd(a.fix_cnt, 1u);
+                    if (gp < a.fix_cap) a.fix_list[gp] = xa;
+                    else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+                }
+            }
+        });
+    }
+    __syncthreads();
+    {
+        uint32_t nf = s_nfix < 256 ? s_nfix : 256;
+        if (tid == 0 && nf) s_fbase = atomicAdd(a.fix_cnt, nf);
+        __syncthreads();
+        for (uint32_t i = tid; i < nf; i += THREADS) {
+            uint32_t gp = s_fbase + i;
+            if (gp < a.fix_cap) a.fix_list[gp] = s_fix[i];
+            else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+        }
+    }
+    // G: store the tile: head bytes, 16-byte body, tail bytes
+    {
+        size_t h_end = (gs + 15) & ~(size_t)15;
+        if (h_end > ge) h_end = ge;
+        size_t b_end = ge & ~(size_t)15;
+        if (b_end < h_end) b_end = h_end;
+        for (size_t g = gs + tid; g < h_end; g += THREADS) a.table[g] = s_tile[g - gal];
+        for (size_t g = h_end + (size_t)tid * 16; g < b_end; g += (size_t)THREADS * 16)
+            *reinterpret_cast<uint4 *>(a.table + g) = *reinterpret_cast<const uint4 *>(s_tile + (g - gal));
+        for (size_t g = b_end + tid; g < ge; g += THREADS) a.table[g] = s_tile[g - gal];
+    }
+}
+
+template <int BPE>
+__global__ void k_fixup_occ(uint8_t *table, const uint32_t *fix_list, const uint32_t *fix_cnt, uint32_t fix_cap)
+{
+    uint32_t nf = min(*fix_cnt, fix_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
+        table[(size_t)fix_list[i] * BPE + (BPE - 1)] |= 4u;
+}
+
+}  // namespace gqf

@@ -1,0 +1,173 @@
+// SQF lookups.
+//
+// The reference (hashAndLookUp, quotientFilter.cu:320-357, with
+// findRunStartGPU :172-196) walks bytes one dependent load at a time: back
+// to the cluster start while `shifted`, then forward counting runs, then
+// through the run.  Here one thread answers one query from 8-slot words:
+// each 8-byte load yields the occupied / continuation / shifted / non-empty
+// masks of 8 slots (SWAR pack), the walk back to the cluster start
+// accumulates D = #occupied - #run-starts in [cluster start, fq), and the
+// query's run is the (D+1)-th run start at or after fq (runs are stored in
+// quotient order, one per occupied quotient).  The run is then scanned in
+// registers.  Result: the slot of the first element of the run whose
+// remainder equals fr, or NOT_FOUND -- the reference's return value.
+#pragma once
+
+#include "qf_device.cuh"
+
+namespace gqf {
+
+struct TableView {
+    const uint8_t *t;
+    uint32_t q, r;
+    uint32_t nslots;      // (1<<q)*1.1
+    uint32_t nbytes;      // table bytes
+    uint32_t nwords_full; // 8-byte words fully inside the table
+};
+
+__device__ __forceinline__ uint64_t ld_word(const TableView &v, uint32_t w)
+{
+    if (w < v.nwords_full) return __ldg(reinterpret_cast<const unsigned long long *>(v.t) + w);
+    uint64_t x = 0;
+    for (uint32_t k = 0; k < 8; k++) {
+        uint32_t i = w * 8 + k;
+        if (i < v.nbytes) x |= (uint64_t)v.t[i] << (8 * k);
+    }
+    return x;
+}
+
+// One query against a table of 1-byte slots (r = 5).
+__device__ __forceinline__ uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr)
+{
+    uint32_t w = fq >> 3, k = fq & 7u;
+    uint64_t x = ld_word(v, w);
+    Flags8 f = flags8(x);
+    if (!((f.occ >> k) & 1u)) return GQF_NOT_FOUND;
+    uint32_t rs = f.nonempty & ~f.cont;   // run starts
+    uint32_t cs = ~f.shift & 0xFFu;       // walk-back stops (not shifted)
+    int D;
+    const uint32_t below = (1u << k) - 1u;
+    uint32_t m = cs & (below | (1u << k));
+    if (m) {
+        uint32_t rng = below & ~((1u << highest_bit(m)) - 1u);
+        D = popc32(f.occ & rng) - popc32(rs & rng);
+    } else {
+        D = popc32(f.occ & below) - popc32(rs & below);
+        for (int ww = (int)w - 1; ww >= 0; ww--) {
+            Flags8 g = flags8(ld_word(v, (uint32_t)ww));
+            uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
+            if (cs2) {
+                uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
+                D += popc32(g.occ & rng) - popc32(rs2 & rng);
+                break;
+            }
+            D += popc32(g.occ) - popc32(rs2);
+        }
+    }
+    // forward: the (D+1)-th run start at or after fq
+    const uint32_t nwords = (v.nslots + 7) >> 3;
+    uint32_t rsm = rs & ~below;
+    uint32_t ws = w;
+    for (;;) {
+        int c = popc32(rsm);
+        if (c > D) break;
+        D -= c;
+        if (++ws >= nwords) return GQF_NOT_FOUND;
+        x = ld_word(v, ws);
+        Flags8 g = flags8(x);
+        rsm = g.nonempty & ~g.cont;
+    }
+    uint32_t lane = (uint32_t)select_bit(rsm, D);
+    uint32_t s = ws * 8 + lane;
+    for (;;) {
+        uint32_t e = (uint32_t)(x >> (8 * lane)) & 0xFFu;
+        uint32_t rem = e >> 3;
+        if (rem == fr) return s;
+        if (rem > fr) return GQF_NOT_FOUND;
+        s++;
+        if (++lane == 8) {
+            lane = 0;
+            if (++ws >= nwords) return GQF_NOT_FOUND;
+            x = ld_word(v, ws);
+        }
+        if (!(((uint32_t)(x >> (8 * lane)) >> 1) & 1u)) return GQF_NOT_FOUND;
+    }
+}
+
+// Generic slot walk for multi-byte slots (r = 13: 2-byte big-endian).
+template <int BPE>
+__device__ __forceinline__ uint32_t sqf_get(const TableView &v, uint32_t i)
+{
+    if (i >= v.nslots) return 0;
+    const uint8_t *p = v.t + (size_t)i * BPE;
+    uint32_t e = p[0];
+    for (int k = 1; k < BPE; k++) e = (e << 8) | p[k];
+    return e;
+}
+
+template <int BPE>
+__device__ __forceinline__ uint32_t sqf_query_generic(const TableView &v, uint32_t fq, uint32_t fr)
+{
+    if (!e_occ(sqf_get<BPE>(v, fq))) return GQF_NOT_FOUND;
+    uint32_t b = fq;
+    while (e_shift(sqf_get<BPE>(v, b)) && b > 0) b--;
+    uint32_t s = b;
+    while (b != fq) {
+        do { s++; } while (e_cont(sqf_get<BPE>(v, s)) && s < v.nslots);
+        do { b++; } while (!e_occ(sqf_get<BPE>(v, b)) && b < v.nslots);
+    }
+    do {
+        uint32_t rem = sqf_get<BPE>(v, s) >> 3;
+        if (rem == fr) return s;
+        if (rem > fr) return GQF_NOT_FOUND;
+        s++;
+    } while (e_cont(sqf_get<BPE>(v, s)));
+    return GQF_NOT_FOUND;
+}
+
+template <int BPE>
+__device__ __forceinline__ uint32_t sqf_query(const TableView &v, uint32_t fp)
+{
+    uint32_t fq = (fp >> v.r) & ((1u << v.q) - 1u);
+    uint32_t fr = fp & ((1u << v.r) - 1u);
+    if (BPE == 1) return sqf_query_b1(v, fq, fr);
+    return sqf_query_generic<BPE>(v, fq, fr);
+}
+
+// launchUnsortedLookups: one thread per query.
+template <int BPE>
+__global__ void __launch_bounds__(256) k_lookup_unsorted(const uint32_t *__restrict__ keys, uint32_t n,
+                                                        TableView v, uint32_t *__restrict__ out)
+{
+    const uint32_t fpmask = (v.q + v.r >= 32) ? 0xFFFFFFFFu : ((1u << (v.q + v.r)) - 1u);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t fp = aphash32(__ldg(keys + i)) & fpmask;
+        out[i] = sqf_query<BPE>(v, fp);
+    }
+}
+
+}  // namespace gqf
+
+#include "sqf_build.cuh"
+
+namespace gqf {
+
+// launchSortedLookups: queries arrive grouped by table region (bucket b
+// holds the queries whose quotient lies in [b*2^tb, (b+1)*2^tb)), so one
+// CTA's probes stay inside one ~2^tb-byte stretch of the table; results go
+// straight to their input positions (the reference sorts them back by
+// index instead, quotientFilter.cu:304-305).
+template <int BPE>
+__global__ void __launch_bounds__(256) k_lookup_bucketed(BucketSrc src, const uint32_t *__restrict__ idx,
+                                                        TableView v, uint32_t *__restrict__ out)
+{
+    const uint32_t b = blockIdx.x;
+    const uint32_t n = src.count(b);
+    const size_t base = src.start(b);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        uint32_t fp = src.items[base + i];
+        out[idx[base + i]] = sqf_query<BPE>(v, fp);
+    }
+}
+
+}  // namespace gqf

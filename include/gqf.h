@@ -1,0 +1,139 @@
+/*
+ * gqf.h -- C ABI of the GB300 quotient-filter engine (libgqf.so).
+ *
+ * Plain C: device pointers, sizes and an opaque CUDA stream (`void*`, NULL =
+ * the legacy default stream, which is what the reference uses).  Every entry
+ * point returns a gqf_status.  When `ms` is non-NULL the call is synchronous
+ * like the reference API (it waits for the work, reports device-side errors
+ * and stores the elapsed device time in *ms); when `ms` is NULL the work is
+ * only enqueued on `stream` and device-side errors are collected later by
+ * gqf_stream_status().
+ *
+ * Each declaration names the reference function it replaces
+ * (owensgroup/GPUQuotientFilters, file:line).  The struct layouts are the
+ * reference's own, so a filter made by either API can be used by the other.
+ */
+#ifndef GQF_H
+#define GQF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gqf_status {
+    GQF_OK = 0,
+    GQF_ERR_ARG = 1,       /* bad q/r, null pointer, negative count        */
+    GQF_ERR_FULL = 2,      /* layout needs more than (1<<q)*1.1 slots       */
+    GQF_ERR_CUDA = 3,      /* a CUDA runtime call failed                    */
+    GQF_ERR_TIMEOUT = 4,   /* a bounded device-side wait ran out            */
+    GQF_ERR_NOMEM = 5,     /* workspace allocation failed                   */
+    GQF_ERR_MISMATCH = 6   /* mergeTwoFilters on filters of different q/r   */
+} gqf_status;
+
+/* Standard quotient filter handle: identical to `struct quotient_filter`
+ * (standardQuotientFilter/GPU_version/quotientFilter.cuh:25-31). */
+typedef struct gqf_sqf {
+    unsigned int qbits;
+    unsigned int rbits;
+    unsigned int bytesPerElement;
+    unsigned char *table; /* device, calcNumSlotsGPU(q, r) bytes */
+} gqf_sqf;
+
+/* Rank-and-select filter handle: identical to `struct
+ * countingQuotientFilterGPU` (rankSelectQuotientFilter/GPU_version/
+ * RSQF.cuh:32-37).  Blocks use the reference's packed layout
+ * (RSQF.cuh:24-30): u8 offset, u64 occupieds, u64 runEnds,
+ * u64 remainders[5] = 57 bytes, and gqf allocates one extra zeroed guard
+ * block after the numBlocks logical ones. */
+typedef struct gqf_rsqf {
+    unsigned int qbits;
+    unsigned int numBlocks;
+    void *blocks;
+} gqf_rsqf;
+
+#define GQF_NOT_FOUND 0xFFFFFFFFu
+#define GQF_RSQF_RBITS 5
+#define GQF_RSQF_BLOCK_BYTES 57
+
+/* ---------------- sizing and hashing (host only, no GPU needed) --------- */
+/* calcNumSlotsGPU, quotientFilter.cu:37-42: table bytes for (q, r) */
+size_t gqf_sqf_table_bytes(unsigned int q, unsigned int r);
+/* (1<<q)*1.1 slots, the bound used by findRunStartGPU (quotientFilter.cu:174) */
+unsigned int gqf_sqf_num_slots(unsigned int q);
+/* Normal_APHash, quotientFilter.cu:134-149 */
+unsigned int gqf_aphash(unsigned int value, unsigned int table_size);
+/* calcNumBlocksGPU, RSQF.cu:27-30 */
+size_t gqf_rsqf_num_blocks(unsigned int q);
+/* MT19937 draws after init_genrand(seed) (mt19937ar.cpp:57,102), skipping
+ * `skip` draws first: the reference drivers' key generator. */
+void gqf_mt19937_fill(uint32_t seed, uint64_t skip, uint32_t *out, uint64_t n);
+const char *gqf_status_string(int status);
+/* Number of kernels this library has launched in this process
+ * (instrumentation; no counterpart in the reference). */
+unsigned long long gqf_kernel_launches(void);
+/* latched device error for `stream` since the last call (waits for it) */
+int gqf_stream_status(void *stream);
+
+/* ---------------- standard quotient filter ------------------------------ */
+/* initFilterGPU, quotientFilter.cu:44-55.  Allocates and ZEROES the table
+ * (the reference leaves it uninitialised; its callers memset it). */
+int gqf_sqf_init(gqf_sqf *qf, unsigned int q, unsigned int r);
+int gqf_sqf_free(gqf_sqf *qf);
+
+/* bulkBuildSegmentedLayouts, quotientFilter.cu:1446-1559.  Rebuilds the
+ * whole table from the n keys (clears it first). */
+int gqf_sqf_bulk_build(const gqf_sqf *qf, int n, const uint32_t *d_keys,
+                       int no_duplicates, void *stream, float *ms);
+
+/* launchUnsortedLookups, quotientFilter.cu:359-381: d_out[i] = slot of
+ * key i's remainder, or GQF_NOT_FOUND. */
+int gqf_sqf_lookup_unsorted(const gqf_sqf *qf, int n, const uint32_t *d_keys,
+                            uint32_t *d_out, void *stream, float *ms);
+
+/* launchSortedLookups, quotientFilter.cu:272-318: same results as the
+ * unsorted lookup, computed over queries grouped by table region. */
+int gqf_sqf_lookup_sorted(const gqf_sqf *qf, int n, const uint32_t *d_keys,
+                          uint32_t *d_out, void *stream, float *ms);
+
+/* insert, quotientFilter.cu:533-634: adds each key's fingerprint unless it
+ * is already present. */
+int gqf_sqf_insert(const gqf_sqf *qf, int n, const uint32_t *d_keys,
+                   void *stream, float *ms);
+
+/* superclusterDeletes, quotientFilter.cu:1202-1297: removes one stored copy
+ * of each key's fingerprint. */
+int gqf_sqf_delete(const gqf_sqf *qf, int n, const uint32_t *d_keys,
+                   void *stream, float *ms);
+
+/* insertViaMerge, quotientFilter.cu:1602-1742 (d_old/n_old are unused by
+ * the algorithm, as in the reference :1604). */
+int gqf_sqf_insert_via_merge(const gqf_sqf *qf, const uint32_t *d_old, int n_old,
+                             const uint32_t *d_new, int n_new, int no_duplicates,
+                             void *stream, float *ms);
+
+/* mergeTwoFilters, quotientFilter.cu:1744-1891: qf1 := qf1 + qf2. */
+int gqf_sqf_merge(const gqf_sqf *qf1, const gqf_sqf *qf2, int no_duplicates,
+                  void *stream, float *ms);
+
+/* ---------------- rank-and-select quotient filter ----------------------- */
+/* initCQFGPU, RSQF.cu:32-40 (zeroed blocks + one guard block) */
+int gqf_rsqf_init(gqf_rsqf *cqf, unsigned int q);
+int gqf_rsqf_free(gqf_rsqf *cqf);
+/* insertGPU, RSQF.cu:882-988: d_ret[i] = slot of the i-th smallest
+ * fingerprint of the batch, or -1 */
+int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
+                    int32_t *d_ret, void *stream, float *ms);
+/* launchLookups, RSQF.cu:411-456 (slot or -1, in input order) */
+int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
+                           int32_t *d_out, void *stream, float *ms);
+/* launchUnsortedLookups, RSQF.cu:540-563 */
+int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
+                             int32_t *d_out, void *stream, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GQF_H */

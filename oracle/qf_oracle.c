@@ -275,10 +275,13 @@ uint32_t or_sqf_lookup_fp(const uint8_t *t, uint32_t q, uint32_t r, uint32_t fp)
 }
 
 /* deleteItemGPU, quotientFilter.cu:1076-1200, applied one item at a time:
- * remove one copy of the fingerprint and shift the cluster left.
+ * remove one copy of the fingerprint and shift the cluster left.  The
+ * run counter b stops at the table end (the reference's loops are unbounded
+ * there, :1120,:1144,:1186; past the last occupied slot b is never read).
  * Returns 1 if a copy was removed. */
 int or_sqf_delete_fp(uint8_t *t, uint32_t q, uint32_t r, uint32_t fp)
 {
+    uint32_t ns = or_sqf_num_slots(q);
     uint32_t fq = (fp >> r) & ((1u << q) - 1u);
     uint32_t fr = fp & ((1u << r) - 1u);
     if (!E_OCC(GET(fq))) return 0;
@@ -287,7 +290,7 @@ int or_sqf_delete_fp(uint8_t *t, uint32_t q, uint32_t r, uint32_t fp)
     uint32_t s = b;
     while (b != fq) {
         do { s++; } while (E_CONT(GET(s)));
-        do { b++; } while (!E_OCC(GET(b)));
+        do { b++; } while (!E_OCC(GET(b)) && b < ns);
     }
     uint32_t run_start = s, rem;
     do {
@@ -298,7 +301,7 @@ int or_sqf_delete_fp(uint8_t *t, uint32_t q, uint32_t r, uint32_t fp)
     } while (E_CONT(GET(s)));
     if (rem != fr) return 0;
     if (!E_CONT(GET(s + 1))) {
-        do { b++; } while (!E_OCC(GET(b)));
+        do { b++; } while (!E_OCC(GET(b)) && b < ns);
     }
     if (s == run_start) {
         if (!E_CONT(GET(s + 1)))
@@ -316,7 +319,7 @@ int or_sqf_delete_fp(uint8_t *t, uint32_t q, uint32_t r, uint32_t fp)
                 SET(s, next & ~4u);
             s++;
         } while (E_CONT(GET(s + 1)));
-        do { b++; } while (!E_OCC(GET(b)));
+        do { b++; } while (!E_OCC(GET(b)) && b < ns);
     }
     SET(s, 0);
     return 1;

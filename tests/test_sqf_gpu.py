@@ -1,0 +1,252 @@
+"""SQF parity on the GPU: every op through the C ABI, compared with the oracle
+(table slot arrays bit-exact, lookup results exact)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+class Filter:
+    def __init__(self, G, torch, q, r):
+        self.G, self.torch, self.q, self.r = G, torch, q, r
+        self.qf = G.initFilterGPU(q, r)
+
+    def __del__(self):
+        try:
+            self.G.freeFilterGPU(self.qf)
+        except Exception:
+            pass
+
+    def build(self, keys, nodup=True):
+        return self.G.bulkBuildSegmentedLayouts(self.qf, keys.size, to_dev(self.torch, keys), nodup)
+
+    def slots(self):
+        return O.sqf_slots(self.G.table_bytes(self.qf), self.q, self.r)
+
+    def raw(self):
+        return self.G.table_bytes(self.qf)
+
+    def lookup(self, keys, sorted_=False):
+        out = self.torch.empty(keys.size, dtype=self.torch.int32, device="cuda")
+        fn = self.G.launchSortedLookups if sorted_ else self.G.launchUnsortedLookups
+        fn(self.qf, keys.size, to_dev(self.torch, keys), out)
+        return from_dev(out)
+
+    def insert(self, keys):
+        return self.G.insert(self.qf, keys.size, to_dev(self.torch, keys))
+
+    def delete(self, keys):
+        return self.G.superclusterDeletes(self.qf, keys.size, to_dev(self.torch, keys))
+
+
+def oracle_build(q, r, keys, nodup=True):
+    t = O.sqf_new(q, r)
+    assert O.sqf_bulk_build(t, q, r, keys, nodup) == 0
+    return t
+
+
+def assert_same_table(f, t):
+    raw = f.raw()
+    if not np.array_equal(raw, t):
+        d = np.nonzero(raw != t)[0]
+        raise AssertionError("%d bytes differ, first at %d: gpu %s oracle %s" %
+                             (d.size, d[0], raw[d[0]:d[0] + 8], t[d[0]:d[0] + 8]))
+
+
+def test_config1_build_lookup_delete(gqf, cuda):
+    from gpuquotientfilters_gb300 import workload as W
+    c = W.config1()
+    q, r = c["q"], c["r"]
+    f = Filter(gqf, cuda, q, r)
+    f.build(c["keys"], True)
+    t = oracle_build(q, r, c["keys"])
+    assert_same_table(f, t)
+    g = GOLDEN["sqf_cpu_version"][0]
+    assert (g["q"], g["n"]) == (15, 19661)
+    assert sha(f.slots().astype(np.uint32)) == g["aphash"]["slots_sha256"]
+    want = O.sqf_lookup(t, q, r, c["lookups"])
+    assert np.array_equal(f.lookup(c["lookups"]), want)
+    assert np.array_equal(f.lookup(c["lookups"], sorted_=True), want)
+    f.delete(c["deletes"])
+    O.sqf_delete(t, q, r, c["deletes"])
+    assert_same_table(f, t)
+    assert np.array_equal(f.lookup(c["lookups"]), O.sqf_lookup(t, q, r, c["lookups"]))
+
+
+@pytest.mark.parametrize("q,r,alpha,seed,nodup", [
+    (15, 5, 0.6, 1, False), (12, 5, 0.9, 2, True), (16, 5, 0.95, 3, True), (18, 5, 0.8, 4, False),
+    (20, 5, 0.5, 5, True), (14, 13, 0.8, 6, True), (16, 13, 0.9, 7, False), (7, 5, 0.8, 8, True),
+    (10, 5, 1.0, 9, True), (22, 5, 0.85, 10, True),
+])
+def test_build_and_lookups(gqf, cuda, q, r, alpha, seed, nodup):
+    n = int(alpha * (1 << q))
+    keys = O.mt_keys(seed, n)
+    f = Filter(gqf, cuda, q, r)
+    f.build(keys, nodup)
+    t = oracle_build(q, r, keys, nodup)
+    assert_same_table(f, t)
+    look = np.concatenate([keys[: n // 2], O.mt_keys(seed, n // 2 + 7, skip=n)])
+    want = O.sqf_lookup(t, q, r, look)
+    assert np.array_equal(f.lookup(look), want)
+    assert np.array_equal(f.lookup(look, sorted_=True), want)
+    assert (want[: n // 2] != O.NOT_FOUND).all()
+
+
+def test_build_reference_arithmetic_count(gqf, cuda):
+    from gpuquotientfilters_gb300 import workload as W
+    q, r = 15, 5
+    n = W.n_keys(q, 0.6, reference_arithmetic=True)
+    keys = O.mt_keys(1, n)
+    f = Filter(gqf, cuda, q, r)
+    f.build(keys, True)
+    assert sha(f.slots().astype(np.uint32)) == GOLDEN["sqf_cpu_version"][1]["aphash"]["slots_sha256"]
+
+
+def test_build_heavy_duplicates(gqf, cuda):
+    q, r = 14, 5
+    base = O.mt_keys(11, 2000)
+    keys = np.repeat(base, 5)  # every fingerprint 5 times
+    keys = np.concatenate([keys, O.mt_keys(12, 3000)])
+    for nodup in (False, True):
+        f = Filter(gqf, cuda, q, r)
+        f.build(keys, nodup)
+        assert_same_table(f, oracle_build(q, r, keys, nodup))
+
+
+def test_build_empty_and_rebuild_clears(gqf, cuda):
+    q, r = 12, 5
+    f = Filter(gqf, cuda, q, r)
+    f.build(O.mt_keys(1, 3000), True)
+    f.build(np.zeros(0, np.uint32), True)
+    assert not f.raw().any()
+    keys = O.mt_keys(2, 1000)
+    f.build(keys, True)
+    assert_same_table(f, oracle_build(q, r, keys))
+
+
+def test_build_overfull_reports_full(gqf, cuda):
+    q, r = 10, 5
+    f = Filter(gqf, cuda, q, r)
+    with pytest.raises(gqf.GQFError) as e:
+        f.build(O.mt_keys(3, 2000), True)
+    assert e.value.status == gqf.GQF_ERR_FULL
+
+
+def test_invalid_arguments(gqf, cuda):
+    with pytest.raises(gqf.GQFError):
+        gqf.initFilterGPU(12, 6)  # (r + 3) % 8 != 0
+    with pytest.raises(gqf.GQFError):
+        gqf.initFilterGPU(27, 5)  # q + r > 31
+
+
+@pytest.mark.parametrize("q,r,alpha,seed,nodup_build", [(14, 5, 0.6, 21, True), (16, 5, 0.8, 22, False),
+                                                        (13, 13, 0.7, 23, True), (18, 5, 0.9, 24, True)])
+def test_insert_and_delete(gqf, cuda, q, r, alpha, seed, nodup_build):
+    n = int(alpha * (1 << q))
+    keys = O.mt_keys(seed, n)
+    if not nodup_build:
+        keys = np.concatenate([keys, keys[: n // 20]])
+    f = Filter(gqf, cuda, q, r)
+    f.build(keys, nodup_build)
+    t = oracle_build(q, r, keys, nodup_build)
+    new = np.concatenate([O.mt_keys(seed, n // 8, skip=n), keys[:100], O.mt_keys(seed, 50, skip=n)])
+    f.insert(new)
+    O.sqf_insert(t, q, r, new)
+    assert_same_table(f, t)
+    dels = np.concatenate([keys[: n // 5], new[:200], O.mt_keys(seed + 99, 300), keys[:10]])
+    f.delete(dels)
+    O.sqf_delete(t, q, r, dels)
+    assert_same_table(f, t)
+    look = np.concatenate([keys[: n // 4], new])
+    assert np.array_equal(f.lookup(look), O.sqf_lookup(t, q, r, look))
+
+
+def test_insert_into_empty_and_empty_batches(gqf, cuda):
+    q, r = 12, 5
+    f = Filter(gqf, cuda, q, r)
+    t = O.sqf_new(q, r)
+    keys = O.mt_keys(5, 2500)
+    f.insert(keys)
+    O.sqf_insert(t, q, r, keys)
+    assert_same_table(f, t)
+    f.insert(np.zeros(0, np.uint32))
+    f.delete(np.zeros(0, np.uint32))
+    assert_same_table(f, t)
+    f.delete(keys)
+    assert not f.raw().any()
+
+
+@pytest.mark.parametrize("nodup", [True, False])
+def test_insert_via_merge_and_merge_two(gqf, cuda, nodup):
+    q, r = 15, 5
+    a = O.mt_keys(31, 12000)
+    b = np.concatenate([O.mt_keys(32, 9000), a[:500]])
+    fa = Filter(gqf, cuda, q, r)
+    fa.build(a, False)
+    ta = oracle_build(q, r, a, False)
+    gqf.insertViaMerge(fa.qf, None, 0, to_dev(cuda, b), b.size, nodup)
+    O.sqf_insert_via_merge(ta, q, r, b, nodup)
+    assert_same_table(fa, ta)
+    f1, f2 = Filter(gqf, cuda, q, r), Filter(gqf, cuda, q, r)
+    f1.build(a, True)
+    f2.build(b, False)
+    t1, t2 = oracle_build(q, r, a, True), oracle_build(q, r, b, False)
+    gqf.mergeTwoFilters(f1.qf, f2.qf, nodup)
+    O.sqf_merge_two(t1, t2, q, r, nodup)
+    assert_same_table(f1, t1)
+    assert_same_table(f2, t2)  # second filter untouched
+
+
+def test_merge_size_mismatch(gqf, cuda):
+    f1, f2 = Filter(gqf, cuda, 12, 5), Filter(gqf, cuda, 13, 5)
+    with pytest.raises(gqf.GQFError) as e:
+        gqf.mergeTwoFilters(f1.qf, f2.qf, True)
+    assert e.value.status == gqf.GQF_ERR_MISMATCH
+
+
+def test_key_equal_to_not_found_sentinel(gqf, cuda):
+    """A key of 0xFFFFFFFF is an ordinary key here (the reference's insert
+    loop never retires it: superclusterBidding returns before bidding,
+    quotientFilter.cu:431-433)."""
+    q, r = 12, 5
+    keys = np.array([0xFFFFFFFF, 1, 2, 3], np.uint32)
+    f = Filter(gqf, cuda, q, r)
+    f.insert(keys)
+    t = O.sqf_new(q, r)
+    O.sqf_insert(t, q, r, keys)
+    assert_same_table(f, t)
+    assert (f.lookup(keys) != O.NOT_FOUND).all()
+
+
+def test_config2_full_size_parity(gqf, cuda):
+    """q=26, r=5, 53,687,091 keys: the whole 73.8 MB table bit-exact with the
+    oracle after the build, a 2^20 insert batch and 2^20 deletes; 2^22 mixed
+    lookups exact (sorted and unsorted)."""
+    from gpuquotientfilters_gb300 import workload as W
+    c = W.config2(n_lookup=1 << 22)
+    q, r = c["q"], c["r"]
+    f = Filter(gqf, cuda, q, r)
+    f.build(c["keys"], True)
+    t = oracle_build(q, r, c["keys"], True)
+    assert_same_table(f, t)
+    want = O.sqf_lookup(t, q, r, c["lookups"])
+    assert np.array_equal(f.lookup(c["lookups"]), want)
+    assert np.array_equal(f.lookup(c["lookups"], sorted_=True), want)
+    f.insert(c["inserts"])
+    O.sqf_insert(t, q, r, c["inserts"])
+    assert_same_table(f, t)
+    f.delete(c["deletes"])
+    O.sqf_delete(t, q, r, c["deletes"])
+    assert_same_table(f, t)
