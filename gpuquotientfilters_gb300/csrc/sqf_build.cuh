@@ -181,29 +181,57 @@ __global__ void __launch_bounds__(THREADS) k_bucket_hist(
 }
 
 // ---------------------------------------------------------------------
-// Look-back over bucket descriptors (single thread).  Returns the slot at
-// which bucket b's items start being laid out (c_in).
+// Decoupled look-back over bucket descriptors, one warp: each round reads
+// the 32 nearest unread predecessors at once (lane l holds bucket j - l),
+// waits until all 32 are published, then folds them far-to-near with an
+// ordered shuffle reduction up to the nearest inclusive descriptor.  Returns (on every lane) the slot
+// at which bucket b's items start (c_in).
 // ---------------------------------------------------------------------
-__device__ inline uint32_t lookback_cin(unsigned long long *status, uint32_t b, uint32_t *err)
+__device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_t b, uint32_t *err)
 {
-    LayoutFn acc{0u, 0u};
-    for (int j = (int)b - 1; j >= 0; j--) {
-        unsigned long long v;
+    const int lane = threadIdx.x & 31;
+    LayoutFn acc{0u, 0u};  // functions of the windows already folded (nearer buckets)
+    int j = (int)b - 1;
+    for (;;) {
+        int idx = j - lane;
+        unsigned long long v = idx >= 0 ? 0ull : lb_pack_inc(0u);  // before bucket 0: slot 0
         uint32_t spins = 0;
+        bool timed_out = false;
         for (;;) {
-            v = ld_acquire_u64(status + j);
-            if (v >> 62) break;
+            if (idx >= 0 && (v >> 62) == 0) v = ld_acquire_u64(status + idx);
+            unsigned pending = __ballot_sync(0xffffffffu, (v >> 62) == 0);
+            if (!pending) break;
             if (++spins > SPIN_LIMIT) {
-                atomicOr(err, DEV_ERR_TIMEOUT);
-                return acc.apply(0u);
+                timed_out = true;
+                break;
             }
-            __nanosleep(64);
+            __nanosleep(32);
         }
-        if ((v >> 62) == 2ull) return acc.apply((uint32_t)(v & LB_VMAX));
-        LayoutFn f{(uint32_t)((v >> 31) & LB_VMAX), (uint32_t)(v & LB_VMAX)};
+        if (timed_out) {
+            if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+            return 0u;
+        }
+        unsigned incm = __ballot_sync(0xffffffffu, (v >> 62) == 2ull);
+        const int L = incm ? __ffs(incm) - 1 : 32;  // nearest inclusive lane
+        // lane function: aggregate map; the inclusive lane becomes the
+        // constant max(c, c_L) (applied to c = 0); lanes past it identity
+        LayoutFn f{0u, 0u};
+        if (lane < L) f = LayoutFn{(uint32_t)((v >> 31) & LB_VMAX), (uint32_t)(v & LB_VMAX)};
+        else if (lane == L) f = LayoutFn{0u, (uint32_t)(v & LB_VMAX)};
+        // ordered reduction: farther lanes (higher index) apply first
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            LayoutFn far;
+            far.n = __shfl_down_sync(0xffffffffu, f.n, o);
+            far.F = __shfl_down_sync(0xffffffffu, f.F, o);
+            if (lane + o < 32 && (lane & (2 * o - 1)) == 0) f = compose(far, f);
+        }
+        f.n = __shfl_sync(0xffffffffu, f.n, 0);
+        f.F = __shfl_sync(0xffffffffu, f.F, 0);
+        if (incm) return acc.apply(f.apply(0u));
         acc = compose(f, acc);
+        j -= 32;
     }
-    return acc.apply(0u);
 }
 
 // u16 counters packed two per u32 word
@@ -457,25 +485,25 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     if (lane == 0) wexcl = LayoutFn{0u, 0u};
     if (lane == 31) s_wfn[wid] = incl;
     __syncthreads();
-    if (tid == 0) {
+    if (wid == 0) {
         LayoutFn acc{0u, 0u};
         for (int w = 0; w < THREADS / 32; w++) {
-            s_wexcl[w] = acc;
+            if (lane == 0) s_wexcl[w] = acc;
             acc = compose(acc, s_wfn[w]);
         }
-        // D: publish, look back, publish inclusive
-        if (acc.n > LB_VMAX / 2 || acc.F > LB_VMAX / 2) atomicOr(a.err, DEV_ERR_FULL);
-        uint32_t cin;
-        if (b == 0) {
-            cin = 0;
-        } else {
-            st_release_u64(a.status + b, lb_pack_agg(acc.n, acc.F));
-            cin = lookback_cin(a.status, b, a.err);
+        // D: publish the aggregate, look back, publish the inclusive value
+        if (lane == 0 && (acc.n > LB_VMAX / 2 || acc.F > LB_VMAX / 2)) atomicOr(a.err, DEV_ERR_FULL);
+        uint32_t cin = 0;
+        if (b != 0) {
+            if (lane == 0) st_release_u64(a.status + b, lb_pack_agg(acc.n, acc.F));
+            cin = lookback_cin_warp(a.status, b, a.err);
         }
         uint32_t cout = acc.apply(cin);
-        st_release_u64(a.status + b, lb_pack_inc(cout));
-        s_cin = cin;
-        s_cout = cout;
+        if (lane == 0) {
+            st_release_u64(a.status + b, lb_pack_inc(cout));
+            s_cin = cin;
+            s_cout = cout;
+        }
     }
     __syncthreads();
     const uint32_t cin = s_cin, cout = s_cout;
