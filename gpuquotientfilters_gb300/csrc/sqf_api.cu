@@ -181,15 +181,15 @@ static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *
 // Extract a table's fingerprints (sorted for canonical tables) into E and
 // bucket them by quotient range.  Count of elements stays on the device.
 template <int BPE>
-static int extract_into(const uint8_t *table, uint32_t nslots, uint32_t r, const BucketGeom &g, Counts3 *tiles,
-                        uint32_t *Q, uint32_t *E, uint32_t *base, uint32_t *cnt, cudaStream_t s)
+static int extract_into(const uint8_t *table, uint32_t nslots, size_t nbytes, uint32_t r, const BucketGeom &g,
+                        Counts3 *tiles, uint32_t *Q, uint32_t *E, uint32_t *base, uint32_t *cnt, cudaStream_t s)
 {
     uint32_t ntiles = (nslots + EXTRACT_TILE - 1) / EXTRACT_TILE;
     count_launches(6);
-    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, tiles);
+    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles);
     k_scan_counts3<<<1, 1024, 0, s>>>(tiles, ntiles);
-    k_occ_list<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, tiles, Q);
-    k_extract<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, r, tiles, Q, E);
+    k_occ_list<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, Q);
+    k_extract<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, r, tiles, Q, E);
     uint32_t grid = (g.nb + 1 + 255) / 256;
     k_sorted_bounds<<<grid, 256, 0, s>>>(E, &tiles[ntiles].ne, g.nb, g.shift, base, cnt);
     k_bounds_to_counts<<<grid, 256, 0, s>>>(base, g.nb, cnt);
@@ -314,12 +314,12 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
         GQF_CK(cudaMemsetAsync(sc.fix_cnt, 0, 4, s));
         BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
         if (needA) {
-            st = extract_into<BPE>(qf->table, tg.nslots, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt, s);
+            st = extract_into<BPE>(qf->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt, s);
             if (st) return st;
             A = BucketSrc{sc.E, sc.abase, 0, sc.acnt};
         }
         if (bFromTable) {
-            st = extract_into<BPE>(qf2->table, tg.nslots, tg.r, p.g, sc.tiles, sc.Q, sc.E2, sc.a2base, sc.a2cnt, s);
+            st = extract_into<BPE>(qf2->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E2, sc.a2base, sc.a2cnt, s);
             if (st) return st;
             B = BucketSrc{sc.E2, sc.a2base, 0, sc.a2cnt};
         } else if (n) {
@@ -356,8 +356,9 @@ static int lookup_unsorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uin
     TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
     if (n > 0) {
         const DeviceInfo &di = device_info(current_device());
-        uint32_t grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)di.sms * 64);
-        k_lookup_unsorted<BPE><<<grid, 256, 0, s>>>(keys, (uint32_t)n, v, out);
+        uint32_t per_block = LOOKUP_THREADS * LOOKUP_QPT;
+        uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)di.sms * 32);
+        k_lookup_unsorted<BPE><<<grid, LOOKUP_THREADS, 0, s>>>(keys, (uint32_t)n, v, out);
         count_launches(1);
     }
     return call_end(ar, s, ms);
@@ -385,7 +386,7 @@ static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint3
         if (st) return st;
         TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
         BucketSrc src{sc.bitems, sc.bbase, 0, sc.bcnt};
-        k_lookup_bucketed<BPE><<<p.g.nb, 256, 0, s>>>(src, sc.bidx, v, out);
+        k_lookup_bucketed<BPE><<<p.g.nb, LOOKUP_THREADS, 0, s>>>(src, sc.bidx, v, out);
         count_launches(1);
     }
     return call_end(ar, s, ms);

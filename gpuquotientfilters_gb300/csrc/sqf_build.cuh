@@ -112,15 +112,18 @@ __global__ void __launch_bounds__(THREADS) k_hash_bucket(
     for (uint32_t i = tid; i < g.nb; i += THREADS) s_cur[i] = 0;
     __syncthreads();
 
+    // all loads first (IPT requests in flight per thread), then hash + count
     uint32_t fp[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; k++) {
         uint32_t j = k * THREADS + tid;
-        fp[k] = 0xFFFFFFFFu;
-        if (j < cnt) {
-            fp[k] = aphash32(__ldg(keys + c0 + j)) & g.fp_mask;
-            atomicAdd(&s_cur[fp[k] >> g.shift], 1u);
-        }
+        fp[k] = j < cnt ? __ldg(keys + c0 + j) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        uint32_t j = k * THREADS + tid;
+        fp[k] = aphash32(fp[k]) & g.fp_mask;
+        if (j < cnt) atomicAdd(&s_cur[fp[k] >> g.shift], 1u);
     }
     __syncthreads();
     // exclusive offsets + one global reservation per non-empty bucket
@@ -171,9 +174,16 @@ __global__ void __launch_bounds__(THREADS) k_bucket_hist(
     const uint32_t cnt = (uint32_t)min((uint64_t)CHUNK, (uint64_t)n - c0);
     for (uint32_t i = threadIdx.x; i < g.nb; i += THREADS) smem_hist[i] = 0;
     __syncthreads();
-    for (uint32_t j = threadIdx.x; j < cnt; j += THREADS) {
-        uint32_t fp = aphash32(__ldg(keys + c0 + j)) & g.fp_mask;
-        atomicAdd(&smem_hist[fp >> g.shift], 1u);
+    uint32_t v[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        uint32_t j = k * THREADS + threadIdx.x;
+        v[k] = j < cnt ? __ldg(keys + c0 + j) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        uint32_t j = k * THREADS + threadIdx.x;
+        if (j < cnt) atomicAdd(&smem_hist[(aphash32(v[k]) & g.fp_mask) >> g.shift], 1u);
     }
     __syncthreads();
     for (uint32_t b = threadIdx.x; b < g.nb; b += THREADS)
@@ -410,7 +420,19 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     // A: counting sort of tagged remainders by local quotient
     for (uint32_t i = tid; i < S / 2 + 4; i += THREADS) s_cnt[i] = 0;
     __syncthreads();
-    for (uint32_t i = tid; i < n; i += THREADS) cnt16_fetch_inc(s_cnt, (item(i) >> a.r) & (S - 1));
+    // items are read in batches of LB per thread so LB loads are in flight
+    constexpr int LB = 8;
+    for (uint32_t i0 = 0; i0 < n; i0 += THREADS * LB) {
+        uint32_t v[LB];
+#pragma unroll
+        for (int k = 0; k < LB; k++) {
+            uint32_t i = i0 + k * THREADS + tid;
+            v[k] = i < n ? item(i) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < LB; k++)
+            if (i0 + k * THREADS + tid < n) cnt16_fetch_inc(s_cnt, (v[k] >> a.r) & (S - 1));
+    }
     __syncthreads();
     // exclusive scan of the u16 counters: thread owns QPT consecutive quotients
     const uint32_t QPT = S / THREADS;  // S >= 2 * THREADS, power of two
@@ -445,10 +467,21 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
         }
     }
     __syncthreads();
-    for (uint32_t i = tid; i < n; i += THREADS) {
-        uint32_t fp = item(i);
-        uint32_t p = cnt16_fetch_inc(s_cnt, (fp >> a.r) & (S - 1));
-        s_rem[p] = (Rem)(((fp & rmask) << 1) | (i >= na ? 1u : 0u));
+    for (uint32_t i0 = 0; i0 < n; i0 += THREADS * LB) {
+        uint32_t v[LB];
+#pragma unroll
+        for (int k = 0; k < LB; k++) {
+            uint32_t i = i0 + k * THREADS + tid;
+            v[k] = i < n ? item(i) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < LB; k++) {
+            uint32_t i = i0 + k * THREADS + tid;
+            if (i < n) {
+                uint32_t p = cnt16_fetch_inc(s_cnt, (v[k] >> a.r) & (S - 1));
+                s_rem[p] = (Rem)(((v[k] & rmask) << 1) | (i >= na ? 1u : 0u));
+            }
+        }
     }
     __syncthreads();
     // s_cnt[x] now holds the END of group x; group x = [end(x-1), end(x))

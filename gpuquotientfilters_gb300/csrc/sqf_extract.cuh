@@ -18,21 +18,41 @@
 namespace gqf {
 
 constexpr int EXTRACT_THREADS = 256;
-constexpr uint32_t EXTRACT_TILE = EXTRACT_THREADS * 8;  // slots per tile
+constexpr int EXTRACT_WPT = 4;  // 8-slot words per thread
+constexpr uint32_t EXTRACT_TILE = EXTRACT_THREADS * EXTRACT_WPT * 8;  // slots per tile
 
 struct Counts3 {
     uint32_t ne, rs, occ;  // non-empty, run starts, occupied
 };
 
+// Element values of 8 consecutive slots starting at slot s0 (zero past the
+// logical end).  One 8-byte load per 8 one-byte slots; two for 2-byte slots.
 template <int BPE>
-__device__ __forceinline__ void load8_elems(const uint8_t *t, uint32_t nslots, uint32_t s0, uint32_t e[8])
+__device__ __forceinline__ void load8_elems(const uint8_t *t, uint32_t nslots, uint32_t nbytes, uint32_t s0,
+                                            uint32_t e[8])
 {
+    if (BPE == 1 && s0 + 8 <= nslots) {
+        uint64_t x = __ldg(reinterpret_cast<const unsigned long long *>(t + s0));
+#pragma unroll
+        for (int k = 0; k < 8; k++) e[k] = (uint32_t)(x >> (8 * k)) & 0xFFu;
+        return;
+    }
+    if (BPE == 2 && s0 + 8 <= nslots && (size_t)(s0 + 8) * 2 <= nbytes) {
+        const unsigned long long *p = reinterpret_cast<const unsigned long long *>(t + (size_t)s0 * 2);
+        uint64_t x0 = __ldg(p), x1 = __ldg(p + 1);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            e[k] = (((uint32_t)(x0 >> (16 * k)) & 0xFFu) << 8) | ((uint32_t)(x0 >> (16 * k + 8)) & 0xFFu);
+            e[k + 4] = (((uint32_t)(x1 >> (16 * k)) & 0xFFu) << 8) | ((uint32_t)(x1 >> (16 * k + 8)) & 0xFFu);
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        uint32_t s = s0 + k;
+        uint32_t sl = s0 + k;
         uint32_t v = 0;
-        if (s < nslots) {
-            const uint8_t *p = t + (size_t)s * BPE;
+        if (sl < nslots) {
+            const uint8_t *p = t + (size_t)sl * BPE;
             v = p[0];
             if (BPE == 2) v = (v << 8) | p[1];
         }
@@ -40,11 +60,8 @@ __device__ __forceinline__ void load8_elems(const uint8_t *t, uint32_t nslots, u
     }
 }
 
-template <int BPE>
-__device__ __forceinline__ void masks8(const uint8_t *t, uint32_t nslots, uint32_t s0, uint32_t &ne, uint32_t &rs,
-                                       uint32_t &occ, uint32_t e[8])
+__device__ __forceinline__ void masks_of(const uint32_t e[8], uint32_t &ne, uint32_t &rs, uint32_t &occ)
 {
-    load8_elems<BPE>(t, nslots, s0, e);
     ne = rs = occ = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -55,25 +72,52 @@ __device__ __forceinline__ void masks8(const uint8_t *t, uint32_t nslots, uint32
     }
 }
 
+// A thread's EXTRACT_WPT words: element values and per-word masks.
+template <int BPE>
+struct ThreadSlots {
+    uint32_t e[EXTRACT_WPT][8];
+    uint32_t ne[EXTRACT_WPT], rs[EXTRACT_WPT], occ[EXTRACT_WPT];
+    uint32_t s0;
+    __device__ __forceinline__ void load(const uint8_t *t, uint32_t nslots, uint32_t nbytes)
+    {
+        s0 = blockIdx.x * EXTRACT_TILE + threadIdx.x * (EXTRACT_WPT * 8);
+#pragma unroll
+        for (int w = 0; w < EXTRACT_WPT; w++) load8_elems<BPE>(t, nslots, nbytes, s0 + 8 * w, e[w]);
+#pragma unroll
+        for (int w = 0; w < EXTRACT_WPT; w++) masks_of(e[w], ne[w], rs[w], occ[w]);
+    }
+    __device__ __forceinline__ Counts3 totals() const
+    {
+        Counts3 c{0, 0, 0};
+#pragma unroll
+        for (int w = 0; w < EXTRACT_WPT; w++) {
+            c.ne += __popc(ne[w]);
+            c.rs += __popc(rs[w]);
+            c.occ += __popc(occ[w]);
+        }
+        return c;
+    }
+};
+
 // Pass 1: per-tile counts.
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_tile_counts(const uint8_t *__restrict__ t, uint32_t nslots,
-                                                                Counts3 *__restrict__ tiles)
+                                                                uint32_t nbytes, Counts3 *__restrict__ tiles)
 {
-    const uint32_t s0 = blockIdx.x * EXTRACT_TILE + threadIdx.x * 8;
-    uint32_t ne, rs, occ, e[8];
-    masks8<BPE>(t, nslots, s0, ne, rs, occ, e);
-    uint32_t a = __popc(ne), b = __popc(rs), c = __popc(occ);
+    ThreadSlots<BPE> ts;
+    ts.load(t, nslots, nbytes);
+    Counts3 c = ts.totals();
+    uint32_t a = c.ne, b = c.rs, d = c.occ;
     for (int o = 16; o; o >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, o);
         b += __shfl_xor_sync(0xffffffffu, b, o);
-        c += __shfl_xor_sync(0xffffffffu, c, o);
+        d += __shfl_xor_sync(0xffffffffu, d, o);
     }
     __shared__ uint32_t sw[3][EXTRACT_THREADS / 32];
     if ((threadIdx.x & 31) == 0) {
         sw[0][threadIdx.x >> 5] = a;
         sw[1][threadIdx.x >> 5] = b;
-        sw[2][threadIdx.x >> 5] = c;
+        sw[2][threadIdx.x >> 5] = d;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -87,33 +131,56 @@ __global__ void __launch_bounds__(EXTRACT_THREADS) k_tile_counts(const uint8_t *
     }
 }
 
-// Exclusive scan of the tile counts by one CTA (tiles <= a few 1e5);
-// total written at tiles[ntiles].
+// Exclusive scan of the tile counts by one CTA; total written at
+// tiles[ntiles].  Each thread loads its run of tiles with independent loads.
 __global__ void __launch_bounds__(1024) k_scan_counts3(Counts3 *tiles, uint32_t ntiles)
 {
-    __shared__ Counts3 s_part[1024];
+    __shared__ uint32_t sw[3][32];
     const uint32_t per = (ntiles + 1023) / 1024;
     const uint32_t beg = min(ntiles, threadIdx.x * per), end = min(ntiles, beg + per);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Counts3 sum{0, 0, 0};
     for (uint32_t i = beg; i < end; i++) {
-        sum.ne += tiles[i].ne;
-        sum.rs += tiles[i].rs;
-        sum.occ += tiles[i].occ;
+        Counts3 c = tiles[i];
+        sum.ne += c.ne;
+        sum.rs += c.rs;
+        sum.occ += c.occ;
     }
-    s_part[threadIdx.x] = sum;
+    uint32_t a = sum.ne, b = sum.rs, d = sum.occ;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t x = __shfl_up_sync(0xffffffffu, a, o), y = __shfl_up_sync(0xffffffffu, b, o),
+                 z = __shfl_up_sync(0xffffffffu, d, o);
+        if (lane >= o) {
+            a += x;
+            b += y;
+            d += z;
+        }
+    }
+    if (lane == 31) {
+        sw[0][wid] = a;
+        sw[1][wid] = b;
+        sw[2][wid] = d;
+    }
     __syncthreads();
-    // Hillis-Steele over 1024 partials
-    for (int o = 1; o < 1024; o <<= 1) {
-        Counts3 v{0, 0, 0};
-        if (threadIdx.x >= (unsigned)o) v = s_part[threadIdx.x - o];
-        __syncthreads();
-        s_part[threadIdx.x].ne += v.ne;
-        s_part[threadIdx.x].rs += v.rs;
-        s_part[threadIdx.x].occ += v.occ;
-        __syncthreads();
+    if (wid == 0) {
+        uint32_t x = sw[0][lane], y = sw[1][lane], z = sw[2][lane];
+        uint32_t ix = x, iy = y, iz = z;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t p = __shfl_up_sync(0xffffffffu, ix, o), q = __shfl_up_sync(0xffffffffu, iy, o),
+                     r = __shfl_up_sync(0xffffffffu, iz, o);
+            if (lane >= o) {
+                ix += p;
+                iy += q;
+                iz += r;
+            }
+        }
+        sw[0][lane] = ix - x;
+        sw[1][lane] = iy - y;
+        sw[2][lane] = iz - z;
+        if (lane == 31) tiles[ntiles] = Counts3{ix, iy, iz};
     }
-    Counts3 run{0, 0, 0};
-    if (threadIdx.x) run = s_part[threadIdx.x - 1];
+    __syncthreads();
+    Counts3 run{sw[0][wid] + a - sum.ne, sw[1][wid] + b - sum.rs, sw[2][wid] + d - sum.occ};
     for (uint32_t i = beg; i < end; i++) {
         Counts3 c = tiles[i];
         tiles[i] = run;
@@ -121,15 +188,14 @@ __global__ void __launch_bounds__(1024) k_scan_counts3(Counts3 *tiles, uint32_t 
         run.rs += c.rs;
         run.occ += c.occ;
     }
-    if (threadIdx.x == 1023) tiles[ntiles] = s_part[1023];
 }
 
 // Block-exclusive prefix of three per-thread counts.
-__device__ __forceinline__ Counts3 block_excl3(uint32_t a, uint32_t b, uint32_t c)
+__device__ __forceinline__ Counts3 block_excl3(Counts3 c)
 {
     __shared__ uint32_t sw[3][EXTRACT_THREADS / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t ia = a, ib = b, ic = c;
+    uint32_t ia = c.ne, ib = c.rs, ic = c.occ;
     for (int o = 1; o < 32; o <<= 1) {
         uint32_t va = __shfl_up_sync(0xffffffffu, ia, o);
         uint32_t vb = __shfl_up_sync(0xffffffffu, ib, o);
@@ -146,7 +212,7 @@ __device__ __forceinline__ Counts3 block_excl3(uint32_t a, uint32_t b, uint32_t 
         sw[2][wid] = ic;
     }
     __syncthreads();
-    Counts3 r{ia - a, ib - b, ic - c};
+    Counts3 r{ia - c.ne, ib - c.rs, ic - c.occ};
     for (int w = 0; w < wid; w++) {
         r.ne += sw[0][w];
         r.rs += sw[1][w];
@@ -160,39 +226,47 @@ __device__ __forceinline__ Counts3 block_excl3(uint32_t a, uint32_t b, uint32_t 
 // the j-th run).
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_occ_list(const uint8_t *__restrict__ t, uint32_t nslots,
-                                                             const Counts3 *__restrict__ tiles, uint32_t *__restrict__ Q)
+                                                             uint32_t nbytes, const Counts3 *__restrict__ tiles,
+                                                             uint32_t *__restrict__ Q)
 {
-    const uint32_t s0 = blockIdx.x * EXTRACT_TILE + threadIdx.x * 8;
-    uint32_t ne, rs, occ, e[8];
-    masks8<BPE>(t, nslots, s0, ne, rs, occ, e);
-    Counts3 ex = block_excl3(__popc(ne), __popc(rs), __popc(occ));
+    ThreadSlots<BPE> ts;
+    ts.load(t, nslots, nbytes);
+    Counts3 ex = block_excl3(ts.totals());
     uint32_t o = tiles[blockIdx.x].occ + ex.occ;
-    while (occ) {
-        int k = __ffs(occ) - 1;
-        occ &= occ - 1;
-        Q[o++] = s0 + k;
+#pragma unroll
+    for (int w = 0; w < EXTRACT_WPT; w++) {
+        uint32_t m = ts.occ[w];
+        while (m) {
+            int k = __ffs(m) - 1;
+            m &= m - 1;
+            Q[o++] = ts.s0 + 8 * w + k;
+        }
     }
 }
 
 // Pass 3: E[i] = fingerprint of the i-th stored element.
 template <int BPE>
-__global__ void __launch_bounds__(EXTRACT_THREADS) k_extract(const uint8_t *__restrict__ t, uint32_t nslots, uint32_t r,
+__global__ void __launch_bounds__(EXTRACT_THREADS) k_extract(const uint8_t *__restrict__ t, uint32_t nslots,
+                                                            uint32_t nbytes, uint32_t r,
                                                             const Counts3 *__restrict__ tiles,
                                                             const uint32_t *__restrict__ Q, uint32_t *__restrict__ E)
 {
-    const uint32_t s0 = blockIdx.x * EXTRACT_TILE + threadIdx.x * 8;
-    uint32_t ne, rs, occ, e[8];
-    masks8<BPE>(t, nslots, s0, ne, rs, occ, e);
-    Counts3 ex = block_excl3(__popc(ne), __popc(rs), __popc(occ));
+    ThreadSlots<BPE> ts;
+    ts.load(t, nslots, nbytes);
+    Counts3 ex = block_excl3(ts.totals());
     uint32_t o = tiles[blockIdx.x].ne + ex.ne;
-    uint32_t runs_before = tiles[blockIdx.x].rs + ex.rs;  // run starts strictly before s0
+    uint32_t runs_before = tiles[blockIdx.x].rs + ex.rs;  // run starts strictly before this thread's slots
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        if (!((ne >> k) & 1u)) continue;
-        uint32_t rs_upto = runs_before + __popc(rs & ((2u << k) - 1u));
-        // rs_upto >= 1 in a valid table (slot 0 of a cluster starts a run)
-        uint32_t j = rs_upto ? rs_upto - 1 : 0;
-        E[o++] = (Q[j] << r) | (e[k] >> 3);
+    for (int w = 0; w < EXTRACT_WPT; w++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            if (!((ts.ne[w] >> k) & 1u)) continue;
+            uint32_t rs_upto = runs_before + __popc(ts.rs[w] & ((2u << k) - 1u));
+            // rs_upto >= 1 in a valid table (the first element of a cluster starts a run)
+            uint32_t j = rs_upto ? rs_upto - 1 : 0;
+            E[o++] = (Q[j] << r) | (ts.e[w][k] >> 3);
+        }
+        runs_before += __popc(ts.rs[w]);
     }
 }
 

@@ -36,11 +36,13 @@ __device__ __forceinline__ uint64_t ld_word(const TableView &v, uint32_t w)
     return x;
 }
 
-// One query against a table of 1-byte slots (r = 5).
-__device__ __forceinline__ uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr)
+// One query against a table of 1-byte slots (r = 5); x0 is the 8-slot word
+// holding slot fq (loaded by the caller so several queries' first loads
+// can be in flight together).
+__device__ __forceinline__ uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr, uint64_t x0)
 {
     uint32_t w = fq >> 3, k = fq & 7u;
-    uint64_t x = ld_word(v, w);
+    uint64_t x = x0;
     Flags8 f = flags8(x);
     if (!((f.occ >> k) & 1u)) return GQF_NOT_FOUND;
     uint32_t rs = f.nonempty & ~f.cont;   // run starts
@@ -130,19 +132,63 @@ __device__ __forceinline__ uint32_t sqf_query(const TableView &v, uint32_t fp)
 {
     uint32_t fq = (fp >> v.r) & ((1u << v.q) - 1u);
     uint32_t fr = fp & ((1u << v.r) - 1u);
-    if (BPE == 1) return sqf_query_b1(v, fq, fr);
+    if (BPE == 1) return sqf_query_b1(v, fq, fr, ld_word(v, fq >> 3));
     return sqf_query_generic<BPE>(v, fq, fr);
 }
 
-// launchUnsortedLookups: one thread per query.
+// Queries per thread in flight in the lookup kernels.
+constexpr int LOOKUP_QPT = 4;
+constexpr int LOOKUP_THREADS = 256;
+
+// QPT queries of one thread: keys loaded together, first table words
+// loaded together, then each walk finishes (rarely needing more words).
 template <int BPE>
-__global__ void __launch_bounds__(256) k_lookup_unsorted(const uint32_t *__restrict__ keys, uint32_t n,
-                                                        TableView v, uint32_t *__restrict__ out)
+__device__ __forceinline__ void sqf_query_batch(const TableView &v, const uint32_t (&fp)[LOOKUP_QPT],
+                                                const bool (&valid)[LOOKUP_QPT], uint32_t (&res)[LOOKUP_QPT])
+{
+    if (BPE == 1) {
+        uint64_t x[LOOKUP_QPT];
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) {
+            uint32_t fq = (fp[k] >> v.r) & ((1u << v.q) - 1u);
+            x[k] = valid[k] ? ld_word(v, fq >> 3) : 0ull;
+        }
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) {
+            uint32_t fq = (fp[k] >> v.r) & ((1u << v.q) - 1u);
+            uint32_t fr = fp[k] & ((1u << v.r) - 1u);
+            res[k] = valid[k] ? sqf_query_b1(v, fq, fr, x[k]) : GQF_NOT_FOUND;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) res[k] = valid[k] ? sqf_query<BPE>(v, fp[k]) : GQF_NOT_FOUND;
+    }
+}
+
+// launchUnsortedLookups: LOOKUP_QPT queries per thread, coalesced keys.
+template <int BPE>
+__global__ void __launch_bounds__(LOOKUP_THREADS) k_lookup_unsorted(const uint32_t *__restrict__ keys, uint32_t n,
+                                                                   TableView v, uint32_t *__restrict__ out)
 {
     const uint32_t fpmask = (v.q + v.r >= 32) ? 0xFFFFFFFFu : ((1u << (v.q + v.r)) - 1u);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t fp = aphash32(__ldg(keys + i)) & fpmask;
-        out[i] = sqf_query<BPE>(v, fp);
+    const uint32_t per_block = LOOKUP_THREADS * LOOKUP_QPT;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * per_block; b0 < n; b0 += (uint64_t)gridDim.x * per_block) {
+        uint32_t fp[LOOKUP_QPT], res[LOOKUP_QPT];
+        bool valid[LOOKUP_QPT];
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) {
+            uint64_t i = b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x;
+            valid[k] = i < n;
+            fp[k] = valid[k] ? __ldg(keys + i) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) fp[k] = aphash32(fp[k]) & fpmask;
+        sqf_query_batch<BPE>(v, fp, valid, res);
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) {
+            uint64_t i = b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x;
+            if (valid[k]) out[i] = res[k];
+        }
     }
 }
 
@@ -158,15 +204,26 @@ namespace gqf {
 // straight to their input positions (the reference sorts them back by
 // index instead, quotientFilter.cu:304-305).
 template <int BPE>
-__global__ void __launch_bounds__(256) k_lookup_bucketed(BucketSrc src, const uint32_t *__restrict__ idx,
-                                                        TableView v, uint32_t *__restrict__ out)
+__global__ void __launch_bounds__(LOOKUP_THREADS) k_lookup_bucketed(BucketSrc src, const uint32_t *__restrict__ idx,
+                                                                   TableView v, uint32_t *__restrict__ out)
 {
     const uint32_t b = blockIdx.x;
     const uint32_t n = src.count(b);
     const size_t base = src.start(b);
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        uint32_t fp = src.items[base + i];
-        out[idx[base + i]] = sqf_query<BPE>(v, fp);
+    for (uint32_t i0 = 0; i0 < n; i0 += LOOKUP_THREADS * LOOKUP_QPT) {
+        uint32_t fp[LOOKUP_QPT], id[LOOKUP_QPT], res[LOOKUP_QPT];
+        bool valid[LOOKUP_QPT];
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++) {
+            uint32_t i = i0 + k * LOOKUP_THREADS + threadIdx.x;
+            valid[k] = i < n;
+            fp[k] = valid[k] ? src.items[base + i] : 0u;
+            id[k] = valid[k] ? idx[base + i] : 0u;
+        }
+        sqf_query_batch<BPE>(v, fp, valid, res);
+#pragma unroll
+        for (int k = 0; k < LOOKUP_QPT; k++)
+            if (valid[k]) out[id[k]] = res[k];
     }
 }
 
