@@ -132,8 +132,12 @@ def run_gpu(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     G.lib()
-    c = W.config2(seed=SEED + 0 * rank)
-    T = G.calcNumSlotsGPU(Q, R)
+    q = args.q
+    n_keys = N_KEYS if q == Q else W.n_keys(q, 0.8)
+    c = W.config2(seed=SEED, q=q, n=n_keys, n_lookup=N_LOOKUP >> (Q - q), n_insert=N_INSERT >> (Q - q),
+                  n_delete=N_DELETE >> (Q - q))
+    n_look, n_ins, n_del = c["lookups"].size, c["inserts"].size, c["deletes"].size
+    T = G.calcNumSlotsGPU(q, R)
 
     def dev_u32(a):
         return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
@@ -142,19 +146,22 @@ def run_gpu(args, world, rank, local):
     d_look = dev_u32(c["lookups"])
     d_ins = dev_u32(c["inserts"])
     d_del = dev_u32(c["deletes"])
-    d_out = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
-    d_out2 = torch.empty(N_LOOKUP, dtype=torch.int32, device=dev)
+    d_out = torch.empty(n_look, dtype=torch.int32, device=dev)
+    d_out2 = torch.empty(n_look, dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
-    qf = G.initFilterGPU(Q, R)
+    qf = G.initFilterGPU(q, R)
     stream = torch.cuda.current_stream(dev)
 
     ops = [
-        ("build", N_KEYS, lambda: G.bulkBuildSegmentedLayouts(qf, N_KEYS, d_keys, True, stream=stream)),
-        ("lookup_unsorted", N_LOOKUP, lambda: G.launchUnsortedLookups(qf, N_LOOKUP, d_look, d_out, stream=stream)),
-        ("lookup_sorted", N_LOOKUP, lambda: G.launchSortedLookups(qf, N_LOOKUP, d_look, d_out2, stream=stream)),
-        ("insert", N_INSERT, lambda: G.insert(qf, N_INSERT, d_ins, stream=stream)),
-        ("delete", N_DELETE, lambda: G.superclusterDeletes(qf, N_DELETE, d_del, stream=stream)),
+        ("build", n_keys, lambda: G.bulkBuildSegmentedLayouts(qf, n_keys, d_keys, True, stream=stream)),
+        ("lookup_unsorted", n_look, lambda: G.launchUnsortedLookups(qf, n_look, d_look, d_out, stream=stream)),
+        ("lookup_sorted", n_look, lambda: G.launchSortedLookups(qf, n_look, d_look, d_out2, stream=stream)),
+        ("insert", n_ins, lambda: G.insert(qf, n_ins, d_ins, stream=stream)),
+        ("delete", n_del, lambda: G.superclusterDeletes(qf, n_del, d_del, stream=stream)),
     ]
+    wanted = args.ops.split(",") if args.ops else None
+    if wanted:
+        ops = [o for o in ops if o[0] in wanted or o[0] == "build"]
 
     def step(record):
         tot = 0.0
@@ -174,7 +181,8 @@ def run_gpu(args, world, rank, local):
     for _ in range(args.warmup):
         step(None)
     # correctness guard on the measured path: sorted == unsorted
-    assert torch.equal(d_out, d_out2), "sorted and unsorted lookups disagree"
+    if not wanted:
+        assert torch.equal(d_out, d_out2), "sorted and unsorted lookups disagree"
 
     clocks = ClockSampler(local)
     rec = {}
@@ -202,7 +210,7 @@ def run_gpu(args, world, rank, local):
     b = per_op["build"]
 
     # end to end through the same API from pinned host buffers
-    e2e = e2e_step(args, G, torch, dev, stream, c, qf)
+    e2e = e2e_step(args, G, torch, dev, stream, c, qf) if not wanted and q == Q else None
     G.freeFilterGPU(qf)
     return {
         "value": value, "ms_per_step": t_max / args.steps, "per_op": per_op, "clocks": clk,
@@ -315,6 +323,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gqf", choices=["gqf", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--q", type=int, default=Q, help="quotient bits (26 = the benchmark workload; smaller "
+                    "values scale every batch by 2^(q-26), for profiling small cases)")
+    ap.add_argument("--ops", default="", help="comma list of ops to run (build always runs)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
