@@ -53,7 +53,7 @@ struct LayoutPlan {
 // Bucket geometry for `n_expect` items over 2^q quotients: about 12k items
 // per bucket (one CTA sorts a bucket in shared memory), at most 4096 buckets
 // (the scatter keeps two u32 per bucket in shared memory).
-static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_t n_b_expect)
+static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_t n_b_expect, bool bitmap)
 {
     const DeviceInfo &di = device_info(current_device());
     LayoutPlan p;
@@ -74,14 +74,19 @@ static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_
     double avg = (double)n_expect / p.g.nb;
     uint32_t need = (uint32_t)(avg * 1.05 + 10.0 * std::sqrt(avg) + 256.0);
     p.threads = (1u << tb) >= 1024 ? 512 : 64;
-    size_t fixed = layout_smem_bytes(tb, 0, bpe);
+    size_t S = (size_t)1 << tb;
+    size_t tile = (S + SPILL_SLOTS) * bpe + 32;
+    size_t counters = 4 * (S / 2 + S / 32 + 8);
+    size_t bitmaps = 4 * (S + S / 32 + 8);
     size_t budget = 100 * 1024;
     size_t maxsm = (size_t)(di.smem_optin > 0 ? di.smem_optin : 99 * 1024) - 4096;
-    if (fixed + (size_t)need * bpe > budget) budget = maxsm;
-    size_t cap = budget > fixed ? (budget - fixed) / bpe : 0;
+    size_t need_bytes = std::max(counters + (size_t)need * bpe, bitmap ? bitmaps : 0) + tile + 16;
+    if (need_bytes > budget) budget = maxsm;
+    size_t r0 = budget > tile + 16 ? budget - tile - 16 : 0;
+    size_t cap = r0 > counters ? (r0 - counters) / bpe : 0;
     cap = std::min<size_t>(cap & ~(size_t)15, 65520);
     p.cap_items = (uint32_t)cap;
-    p.smem = layout_smem_bytes(tb, p.cap_items, bpe);
+    p.smem = layout_smem_bytes(tb, p.cap_items, bpe, bitmap);
     return p;
 }
 
@@ -116,6 +121,7 @@ struct Scratch {
     unsigned long long *status;  // nb  : look-back descriptors
     uint32_t *ticket;
     uint32_t *fix_cnt;
+    uint32_t *a_dups;  // table holds duplicate fingerprints (set by extraction)
     uint32_t *bbase;  // nb+1: exact batch bases
     uint32_t *fix_list;
     uint32_t fix_cap;
@@ -146,6 +152,7 @@ static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *
         s.status = c.template take<unsigned long long>(nb, 8);
         s.ticket = c.template take<uint32_t>(1, 4);
         s.fix_cnt = c.template take<uint32_t>(1, 4);
+        s.a_dups = c.template take<uint32_t>(1, 4);
         s.ctrl_bytes = c.off;
         s.bbase = c.template take<uint32_t>(nb + 1);
         s.fix_cap = std::max<uint32_t>(65536u, r.nslots / 8);
@@ -182,11 +189,12 @@ static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *
 // bucket them by quotient range.  Count of elements stays on the device.
 template <int BPE>
 static int extract_into(const uint8_t *table, uint32_t nslots, size_t nbytes, uint32_t r, const BucketGeom &g,
-                        Counts3 *tiles, uint32_t *Q, uint32_t *E, uint32_t *base, uint32_t *cnt, cudaStream_t s)
+                        Counts3 *tiles, uint32_t *Q, uint32_t *E, uint32_t *base, uint32_t *cnt, uint32_t *dups,
+                        cudaStream_t s)
 {
     uint32_t ntiles = (nslots + EXTRACT_TILE - 1) / EXTRACT_TILE;
     count_launches(6);
-    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles);
+    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, dups);
     k_scan_counts3<<<1, 1024, 0, s>>>(tiles, ntiles);
     k_occ_list<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, Q);
     k_extract<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, r, tiles, Q, E);
@@ -230,7 +238,8 @@ static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, S
 
 template <int BPE>
 static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table, const BucketSrc &A,
-                         const BucketSrc &B, int op, int nodup, Scratch &sc, uint32_t *err, cudaStream_t s)
+                         const BucketSrc &B, int op, int nodup, bool bitmap_ok, const uint32_t *a_dups, Scratch &sc,
+                         uint32_t *err, cudaStream_t s)
 {
     // slots past the last bucket's quotients only receive spill: clear them
     size_t tail = (size_t)(1u << tg.q) * BPE;
@@ -247,6 +256,8 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
     a.cap_items = p.cap_items;
     a.op = op;
     a.nodup = nodup;
+    a.bitmap_ok = bitmap_ok ? 1 : 0;
+    a.a_dups = a_dups;
     a.status = sc.status;
     a.ticket = sc.ticket;
     a.fix_list = sc.fix_list;
@@ -285,7 +296,10 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
     // expected items: the table holds at most nslots
     uint64_t expect = std::min<uint64_t>((needA ? (uint64_t)(tg.nslots * 0.9) : 0) + (bFromTable ? (uint64_t)(tg.nslots * 0.9) : n),
                                          (uint64_t)tg.nslots * 2);
-    LayoutPlan p = plan_layout(tg.q, tg.r, expect, bFromTable ? 0 : n);
+    // r = 5 and set semantics: remainder bitmaps (see LayoutArgs::bitmap_ok)
+    const bool bitmap_ok = tg.r == 5 && (((op == OP_BUILD || op == OP_MERGE) && nodup) || op == OP_INSERT ||
+                                         op == OP_DELETE);
+    LayoutPlan p = plan_layout(tg.q, tg.r, expect, bFromTable ? 0 : n, bitmap_ok);
     ScratchReq req{p.g.nb, bFromTable ? 0 : (size_t)p.g.nb * p.stride, false, needA, bFromTable, tg.nslots};
     (void)nA;
     (void)nB;
@@ -314,12 +328,14 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
         GQF_CK(cudaMemsetAsync(sc.fix_cnt, 0, 4, s));
         BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
         if (needA) {
-            st = extract_into<BPE>(qf->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt, s);
+            st = extract_into<BPE>(qf->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt,
+                                   sc.a_dups, s);
             if (st) return st;
             A = BucketSrc{sc.E, sc.abase, 0, sc.acnt};
         }
         if (bFromTable) {
-            st = extract_into<BPE>(qf2->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E2, sc.a2base, sc.a2cnt, s);
+            st = extract_into<BPE>(qf2->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E2, sc.a2base, sc.a2cnt,
+                                   nullptr, s);
             if (st) return st;
             B = BucketSrc{sc.E2, sc.a2base, 0, sc.a2cnt};
         } else if (n) {
@@ -327,7 +343,8 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
             if (st) return st;
             B = exact ? BucketSrc{sc.bitems, sc.bbase, 0, sc.bcnt} : BucketSrc{sc.bitems, nullptr, p.stride, sc.bcnt};
         }
-        st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, sc, ar.err, s);
+        st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, bitmap_ok,
+                                (op == OP_INSERT || op == OP_DELETE) ? sc.a_dups : nullptr, sc, ar.err, s);
         if (st) return st;
         if (!ms) return call_end(ar, s, nullptr);
         // synchronous: look at the error word before deciding
@@ -368,7 +385,7 @@ template <int BPE>
 static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint32_t *out, cudaStream_t s, float *ms)
 {
     const SqfGeom tg = geom_of(qf);
-    LayoutPlan p = plan_layout(tg.q, tg.r, (uint64_t)tg.nslots * 8 / 10, (uint64_t)n);
+    LayoutPlan p = plan_layout(tg.q, tg.r, (uint64_t)tg.nslots * 8 / 10, (uint64_t)n, false);
     // query buckets: aim for ~4k queries per bucket, table-aligned
     ScratchReq req{p.g.nb, (size_t)std::max(n, 1), true, false, false, tg.nslots};
     Arena &ar = arena(current_device());

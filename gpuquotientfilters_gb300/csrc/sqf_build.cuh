@@ -244,14 +244,20 @@ __device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_
     }
 }
 
-// u16 counters packed two per u32 word
+// Shared-memory word skews: a thread that owns a run of consecutive words
+// starts 17 (resp. 33) words after its neighbour, so the lanes of a warp
+// stepping through their runs hit distinct banks.
+__device__ __forceinline__ uint32_t skew16(uint32_t w) { return w + (w >> 4); }
+__device__ __forceinline__ uint32_t skew32(uint32_t w) { return w + (w >> 5); }
+
+// u16 counters packed two per (skewed) u32 word
 __device__ __forceinline__ uint32_t cnt16_get(const uint32_t *a, uint32_t i)
 {
-    return (a[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+    return (a[skew16(i >> 1)] >> ((i & 1) * 16)) & 0xFFFFu;
 }
 __device__ __forceinline__ uint32_t cnt16_fetch_inc(uint32_t *a, uint32_t i)
 {
-    uint32_t old = atomicAdd(a + (i >> 1), 1u << ((i & 1) * 16));
+    uint32_t old = atomicAdd(a + skew16(i >> 1), 1u << ((i & 1) * 16));
     return (old >> ((i & 1) * 16)) & 0xFFFFu;
 }
 
@@ -328,8 +334,14 @@ struct LayoutArgs {
     BucketSrc A, B;
     uint8_t *table;
     uint32_t q, r, tb, nb, nslots;
-    uint32_t cap_items;  // tagged remainders one CTA can hold
+    uint32_t cap_items;  // tagged remainders one CTA can hold (general mode)
     int op, nodup;
+    // Remainder-bitmap mode: r = 5 and the op has set semantics (NoDup
+    // build/merge, insert/delete into a table without duplicate
+    // fingerprints); `a_dups` (device flag, may be null) vetoes it at run
+    // time when the table holds duplicates.
+    int bitmap_ok;
+    const uint32_t *a_dups;
     unsigned long long *status;
     uint32_t *ticket;
     uint32_t *fix_list;
@@ -338,17 +350,24 @@ struct LayoutArgs {
     uint32_t *err;
 };
 
-// Shared-memory bytes of k_bucket_layout for a geometry.
-__host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_items, int bpe)
+// Shared-memory plan of k_bucket_layout: region 0 holds either the
+// remainder bitmaps (one u32 per quotient) or the packed u16 group counters
+// plus the tagged remainders; the tile buffer follows.
+__host__ __device__ inline size_t layout_region0_bytes(uint32_t tb, uint32_t cap_items, int bpe, bool bitmap)
 {
     size_t S = (size_t)1 << tb;
-    size_t cnt = S * 2 + 16;  // packed u16 counters (+ spare words)
-    size_t rem = ((size_t)cap_items * bpe + 15) & ~(size_t)15;
-    size_t tile = (S + SPILL_SLOTS) * bpe + 32;
-    return cnt + rem + tile;
+    size_t gen = 4 * (S / 2 + S / 32 + 8) + (((size_t)cap_items * bpe + 15) & ~(size_t)15);
+    size_t bit = 4 * (S + S / 32 + 8);
+    return bitmap && bit > gen ? bit : gen;
+}
+__host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_items, int bpe, bool bitmap)
+{
+    size_t S = (size_t)1 << tb;
+    size_t r0 = (layout_region0_bytes(tb, cap_items, bpe, bitmap) + 15) & ~(size_t)15;
+    return r0 + (S + SPILL_SLOTS) * bpe + 32;
 }
 
-// Walks the groups of quotients [qb, qb+QPT) in slot order and calls
+// Group walk (general mode): quotients [qb, qb+QPT) in slot order, calling
 // emit(xa, rem, k) for every item the rebuilt table holds (k = index of the
 // item within its quotient's run).  Groups hold (rem << 1 | source) sorted.
 template <typename Rem, typename Emit>
@@ -371,6 +390,22 @@ __device__ __forceinline__ void walk_groups(const uint32_t *s_cnt, const Rem *s_
     }
 }
 
+// Bitmap walk: bit v of s_mask[skew32(x)] = remainder v kept at quotient x.
+template <typename Emit>
+__device__ __forceinline__ void walk_bits(const uint32_t *s_mask, uint32_t qb, uint32_t QPT, uint32_t x0, Emit &&emit)
+{
+    for (uint32_t j = 0; j < QPT; j++) {
+        uint32_t x = qb + j;
+        uint32_t m = s_mask[skew32(x)];
+        uint32_t kk = 0;
+        while (m) {
+            uint32_t v = (uint32_t)__ffs(m) - 1u;
+            m &= m - 1u;
+            emit(x0 + x, v, kk++);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------
 // K2: one CTA per bucket (taken in ticket order for the look-back).
 // ---------------------------------------------------------------------
@@ -380,10 +415,12 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     using Rem = typename std::conditional<BPE == 1, uint8_t, uint16_t>::type;
     extern __shared__ __align__(16) uint8_t smem_layout[];
     const uint32_t S = 1u << a.tb;
-    uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem_layout);  // S/2 + 4 words
-    Rem *s_rem = reinterpret_cast<Rem *>(smem_layout + (size_t)S * 2 + 16);
-    uint8_t *s_tile = smem_layout + (size_t)S * 2 + 16 +
-                      (((size_t)a.cap_items * BPE + 15) & ~(size_t)15);
+    const bool bitmap = BPE == 1 && a.bitmap_ok && !(a.a_dups && *a.a_dups);
+    uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem_layout);   // general: u16 counters
+    uint32_t *s_mask = reinterpret_cast<uint32_t *>(smem_layout);  // bitmap: u32 per quotient
+    Rem *s_rem = reinterpret_cast<Rem *>(smem_layout + 4 * ((size_t)S / 2 + S / 32 + 8));
+    uint8_t *s_tile = smem_layout + ((layout_region0_bytes(a.tb, a.cap_items, BPE, a.bitmap_ok != 0) + 15) &
+                                     ~(size_t)15);
     const uint32_t BUF = S + SPILL_SLOTS;  // slots the tile buffer holds
 
     __shared__ uint32_t s_warp[33];
@@ -404,8 +441,10 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     const size_t abase = na ? a.A.start(b) : 0, bbase = nbn ? a.B.start(b) : 0;
     const uint32_t x0 = b * S;  // first quotient of the bucket
     const uint32_t rmask = (1u << a.r) - 1u;
+    const uint32_t QPT = S / THREADS;  // S >= 2 * THREADS, power of two
+    const uint32_t qb = tid * QPT;
 
-    if (n > a.cap_items) {
+    if (!bitmap && n > a.cap_items) {
         // cannot sort here: flag it (the host falls back) and keep the chain alive
         if (tid == 0) {
             atomicOr(a.err, DEV_ERR_BUCKET_CAP);
@@ -416,86 +455,116 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     auto item = [&](uint32_t i) -> uint32_t {
         return i < na ? a.A.items[abase + i] : a.B.items[bbase + (i - na)];
     };
-
-    // A: counting sort of tagged remainders by local quotient
-    for (uint32_t i = tid; i < S / 2 + 4; i += THREADS) s_cnt[i] = 0;
-    __syncthreads();
     // items are read in batches of LB per thread so LB loads are in flight
     constexpr int LB = 8;
-    for (uint32_t i0 = 0; i0 < n; i0 += THREADS * LB) {
-        uint32_t v[LB];
-#pragma unroll
-        for (int k = 0; k < LB; k++) {
-            uint32_t i = i0 + k * THREADS + tid;
-            v[k] = i < n ? item(i) : 0u;
-        }
-#pragma unroll
-        for (int k = 0; k < LB; k++)
-            if (i0 + k * THREADS + tid < n) cnt16_fetch_inc(s_cnt, (v[k] >> a.r) & (S - 1));
-    }
-    __syncthreads();
-    // exclusive scan of the u16 counters: thread owns QPT consecutive quotients
-    const uint32_t QPT = S / THREADS;  // S >= 2 * THREADS, power of two
-    const uint32_t qb = tid * QPT;
-    {
-        uint32_t sum = 0;
-        for (uint32_t j = 0; j < QPT; j++) sum += cnt16_get(s_cnt, qb + j);
-        uint32_t incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) s_warp[wid] = incl;
+
+    if (bitmap) {
+        // A: remainder sets by quotient (A first, then B)
+        for (uint32_t i = tid; i < S + S / 32 + 8; i += THREADS) s_mask[i] = 0;
         __syncthreads();
-        if (wid == 0) {
-            uint32_t v = lane < THREADS / 32 ? s_warp[lane] : 0;
-            uint32_t iv = v;
+        for (int src = 0; src < 2; src++) {
+            const uint32_t lo_i = src ? na : 0u, hi_i = src ? n : na;
+            const bool clear = src == 1 && a.op == OP_DELETE;
+            for (uint32_t i0 = lo_i; i0 < hi_i; i0 += THREADS * LB) {
+                uint32_t v[LB];
+#pragma unroll
+                for (int k = 0; k < LB; k++) {
+                    uint32_t i = i0 + k * THREADS + tid;
+                    v[k] = i < hi_i ? item(i) : 0u;
+                }
+#pragma unroll
+                for (int k = 0; k < LB; k++) {
+                    if (i0 + k * THREADS + tid < hi_i) {
+                        uint32_t w = skew32((v[k] >> a.r) & (S - 1)), bit = 1u << (v[k] & rmask);
+                        if (clear) atomicAnd(s_mask + w, ~bit);
+                        else atomicOr(s_mask + w, bit);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    } else {
+        // A: counting sort of tagged remainders by local quotient
+        for (uint32_t i = tid; i < S / 2 + S / 32 + 8; i += THREADS) s_cnt[i] = 0;
+        __syncthreads();
+        for (uint32_t i0 = 0; i0 < n; i0 += THREADS * LB) {
+            uint32_t v[LB];
+#pragma unroll
+            for (int k = 0; k < LB; k++) {
+                uint32_t i = i0 + k * THREADS + tid;
+                v[k] = i < n ? item(i) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < LB; k++)
+                if (i0 + k * THREADS + tid < n) cnt16_fetch_inc(s_cnt, (v[k] >> a.r) & (S - 1));
+        }
+        __syncthreads();
+        // exclusive scan of the u16 counters: thread owns QPT consecutive quotients
+        {
+            uint32_t sum = 0;
+            for (uint32_t j = 0; j < QPT; j++) sum += cnt16_get(s_cnt, qb + j);
+            uint32_t incl = sum;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                uint32_t t = __shfl_up_sync(0xffffffffu, iv, o);
-                if (lane >= o) iv += t;
+                uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
             }
-            if (lane < THREADS / 32) s_warp[lane] = iv - v;
+            if (lane == 31) s_warp[wid] = incl;
+            __syncthreads();
+            if (wid == 0) {
+                uint32_t v = lane < THREADS / 32 ? s_warp[lane] : 0;
+                uint32_t iv = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t t = __shfl_up_sync(0xffffffffu, iv, o);
+                    if (lane >= o) iv += t;
+                }
+                if (lane < THREADS / 32) s_warp[lane] = iv - v;
+            }
+            __syncthreads();
+            uint32_t run = s_warp[wid] + incl - sum;
+            for (uint32_t j = 0; j < QPT; j += 2) {  // QPT even: whole words
+                uint32_t c0 = cnt16_get(s_cnt, qb + j), c1 = cnt16_get(s_cnt, qb + j + 1);
+                s_cnt[skew16((qb + j) >> 1)] = run | ((run + c0) << 16);
+                run += c0 + c1;
+            }
         }
         __syncthreads();
-        uint32_t run = s_warp[wid] + incl - sum;
-        for (uint32_t j = 0; j < QPT; j += 2) {  // QPT even: whole words
-            uint32_t c0 = cnt16_get(s_cnt, qb + j), c1 = cnt16_get(s_cnt, qb + j + 1);
-            s_cnt[(qb + j) >> 1] = run | ((run + c0) << 16);
-            run += c0 + c1;
-        }
-    }
-    __syncthreads();
-    for (uint32_t i0 = 0; i0 < n; i0 += THREADS * LB) {
-        uint32_t v[LB];
+        for (uint32_t i0 = 0; i0 < n; i0 += THREADS * LB) {
+            uint32_t v[LB];
 #pragma unroll
-        for (int k = 0; k < LB; k++) {
-            uint32_t i = i0 + k * THREADS + tid;
-            v[k] = i < n ? item(i) : 0u;
-        }
+            for (int k = 0; k < LB; k++) {
+                uint32_t i = i0 + k * THREADS + tid;
+                v[k] = i < n ? item(i) : 0u;
+            }
 #pragma unroll
-        for (int k = 0; k < LB; k++) {
-            uint32_t i = i0 + k * THREADS + tid;
-            if (i < n) {
-                uint32_t p = cnt16_fetch_inc(s_cnt, (v[k] >> a.r) & (S - 1));
-                s_rem[p] = (Rem)(((v[k] & rmask) << 1) | (i >= na ? 1u : 0u));
+            for (int k = 0; k < LB; k++) {
+                uint32_t i = i0 + k * THREADS + tid;
+                if (i < n) {
+                    uint32_t p = cnt16_fetch_inc(s_cnt, (v[k] >> a.r) & (S - 1));
+                    s_rem[p] = (Rem)(((v[k] & rmask) << 1) | (i >= na ? 1u : 0u));
+                }
             }
         }
-    }
-    __syncthreads();
-    // s_cnt[x] now holds the END of group x; group x = [end(x-1), end(x))
-
-    // B: sort each group; walk the recurrence once from slot 0
-    LayoutFn fn{0u, 0u};
-    {
+        __syncthreads();
+        // s_cnt[x] now holds the END of group x; group x = [end(x-1), end(x))
         for (uint32_t j = 0; j < QPT; j++) {
             uint32_t x = qb + j;
             uint32_t g0 = x ? cnt16_get(s_cnt, x - 1) : 0u, g1 = cnt16_get(s_cnt, x);
             if (g1 - g0 > 1) small_sort(s_rem + g0, g1 - g0);
         }
+    }
+    // every item the rebuilt bucket keeps, in slot order, for this thread
+    auto walk = [&](auto &&emit) {
+        if (bitmap) walk_bits(s_mask, qb, QPT, x0, emit);
+        else walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, emit);
+    };
+
+    // B: this thread's layout map (slot recurrence from slot 0)
+    LayoutFn fn{0u, 0u};
+    {
         uint32_t c = 0, cnt_items = 0;
-        walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, [&](uint32_t xa, uint32_t, uint32_t) {
+        walk([&](uint32_t xa, uint32_t, uint32_t) {
             uint32_t pos = xa > c ? xa : c;
             c = pos + 1;
             cnt_items++;
@@ -559,7 +628,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     // E: emit elements
     {
         uint32_t c = texcl.apply(cin);
-        walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, [&](uint32_t xa, uint32_t rem, uint32_t kk) {
+        walk([&](uint32_t xa, uint32_t rem, uint32_t kk) {
             uint32_t pos = xa > c ? xa : c;
             c = pos + 1;
             if (pos >= hi) return;  // past the table: reported as FULL
@@ -576,25 +645,21 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     __syncthreads();
     // F: occupied bits (own tile) or fix-ups (slot written by an earlier
     // bucket); a quotient is occupied iff the rebuilt group is non-empty
-    {
-        uint32_t last_x = 0xFFFFFFFFu;
-        walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, [&](uint32_t xa, uint32_t, uint32_t kk) {
-            if (kk != 0 || xa == last_x) return;
-            last_x = xa;
-            if (xa >= lo) {
-                s_tile[(size_t)xa * BPE + (BPE - 1) - gal] |= 4u;
+    walk([&](uint32_t xa, uint32_t, uint32_t kk) {
+        if (kk != 0) return;
+        if (xa >= lo) {
+            s_tile[(size_t)xa * BPE + (BPE - 1) - gal] |= 4u;
+        } else {
+            uint32_t p = atomicAdd(&s_nfix, 1u);
+            if (p < 256) {
+                s_fix[p] = xa;
             } else {
-                uint32_t p = atomicAdd(&s_nfix, 1u);
-                if (p < 256) {
-                    s_fix[p] = xa;
-                } else {
-                    uint32_t gp = atomicAdd(a.fix_cnt, 1u);
-                    if (gp < a.fix_cap) a.fix_list[gp] = xa;
-                    else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
-                }
+                uint32_t gp = atomicAdd(a.fix_cnt, 1u);
+                if (gp < a.fix_cap) a.fix_list[gp] = xa;
+                else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
             }
-        });
-    }
+        }
+    });
     __syncthreads();
     {
         uint32_t nf = s_nfix < 256 ? s_nfix : 256;

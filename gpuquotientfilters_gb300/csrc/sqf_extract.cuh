@@ -100,12 +100,33 @@ struct ThreadSlots {
 };
 
 // Pass 1: per-tile counts.
+// When `dups` is non-null it is set to 1 if the table stores a fingerprint
+// twice: a continuation element whose remainder equals its predecessor's.
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_tile_counts(const uint8_t *__restrict__ t, uint32_t nslots,
-                                                                uint32_t nbytes, Counts3 *__restrict__ tiles)
+                                                                uint32_t nbytes, Counts3 *__restrict__ tiles,
+                                                                uint32_t *__restrict__ dups)
 {
     ThreadSlots<BPE> ts;
     ts.load(t, nslots, nbytes);
+    if (dups) {
+        uint32_t prev = 0;
+        if (ts.s0 > 0 && ts.s0 - 1 < nslots) {
+            const uint8_t *p = t + (size_t)(ts.s0 - 1) * BPE;
+            prev = p[0];
+            if (BPE == 2) prev = (prev << 8) | p[1];
+        }
+        bool d = false;
+#pragma unroll
+        for (int w = 0; w < EXTRACT_WPT; w++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                uint32_t e = ts.e[w][k];
+                d |= (e & 2u) && (e >> 3) == (prev >> 3);
+                prev = e;
+            }
+        if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) atomicOr(dups, 1u);
+    }
     Counts3 c = ts.totals();
     uint32_t a = c.ne, b = c.rs, d = c.occ;
     for (int o = 16; o; o >>= 1) {

@@ -250,3 +250,24 @@ def test_config2_full_size_parity(gqf, cuda):
     f.delete(c["deletes"])
     O.sqf_delete(t, q, r, c["deletes"])
     assert_same_table(f, t)
+
+
+def test_skewed_bucket_set_semantics(gqf, cuda):
+    """Thousands of fingerprints in one narrow quotient range (one bucket far
+    over its average): the set-semantics paths handle any bucket size."""
+    q, r = 16, 5
+    cand = O.mt_keys(77, 400000)
+    fps = O.aphash(cand, q, r)
+    sel = cand[(fps >> r) < 3000][:2500]  # quotients 0..2999, ~0.83 per slot
+    keys = np.concatenate([sel, O.mt_keys(78, 20000)])
+    f = Filter(gqf, cuda, q, r)
+    f.build(keys, True)
+    t = oracle_build(q, r, keys, True)
+    assert_same_table(f, t)
+    more = cand[(fps >> r) < 3000][2500:3000]
+    f.insert(more)
+    O.sqf_insert(t, q, r, more)
+    assert_same_table(f, t)
+    f.delete(sel[:1000])
+    O.sqf_delete(t, q, r, sel[:1000])
+    assert_same_table(f, t)
