@@ -75,7 +75,7 @@ static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_
     uint32_t need = (uint32_t)(avg * 1.05 + 10.0 * std::sqrt(avg) + 256.0);
     p.threads = (1u << tb) >= 1024 ? 512 : 64;
     size_t S = (size_t)1 << tb;
-    size_t tile = (S + SPILL_SLOTS) * bpe + 32;
+    size_t tile = (((S + SPILL_SLOTS) * bpe + 32 + 15) & ~(size_t)15) + S / 8;
     size_t counters = 4 * (S / 2 + S / 32 + 8);
     size_t bitmaps = 4 * (S + S / 32 + 8);
     size_t budget = 100 * 1024;
@@ -92,7 +92,7 @@ static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_
 
 static size_t scatter_smem(uint32_t nb, bool pairs)
 {
-    size_t chunk = (size_t)SCATTER_THREADS * SCATTER_IPT;
+    size_t chunk = pairs ? (size_t)PAIR_THREADS * PAIR_IPT : (size_t)SCATTER_THREADS * SCATTER_IPT;
     return (pairs ? 2 : 1) * chunk * 4 + (size_t)nb * 8;
 }
 
@@ -210,27 +210,28 @@ static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, S
                         uint32_t *err, cudaStream_t s)
 {
     if (n == 0) return GQF_OK;
-    const uint32_t chunk = SCATTER_THREADS * SCATTER_IPT;
+    const uint32_t chunk = pairs ? PAIR_THREADS * PAIR_IPT : SCATTER_THREADS * SCATTER_IPT;
     const uint32_t grid = (n + chunk - 1) / chunk;
     const size_t sm = scatter_smem(p.g.nb, pairs);
     if (exact) {
-        GQF_CK(set_smem(k_bucket_hist<SCATTER_THREADS, SCATTER_IPT>, p.g.nb * 4));
         count_launches(2);
-        k_bucket_hist<SCATTER_THREADS, SCATTER_IPT><<<grid, SCATTER_THREADS, p.g.nb * 4, s>>>(keys, n, p.g, sc.bcnt);
+        GQF_CK(set_smem(k_bucket_hist<SCATTER_THREADS, SCATTER_IPT>, p.g.nb * 4));
+        const uint32_t hgrid = (n + SCATTER_THREADS * SCATTER_IPT - 1) / (SCATTER_THREADS * SCATTER_IPT);
+        k_bucket_hist<SCATTER_THREADS, SCATTER_IPT><<<hgrid, SCATTER_THREADS, p.g.nb * 4, s>>>(keys, n, p.g, sc.bcnt);
         k_scan_bases<<<1, 1024, 0, s>>>(sc.bcnt, p.g.nb, sc.bbase);
         GQF_CK(cudaMemsetAsync(sc.bcnt, 0, p.g.nb * 4, s));
     }
     count_launches(1);
     if (pairs) {
-        auto kfn = k_hash_bucket<SCATTER_THREADS, SCATTER_IPT, true>;
+        auto kfn = k_hash_bucket<PAIR_THREADS, PAIR_IPT, true>;
         GQF_CK(set_smem(kfn, sm));
-        kfn<<<grid, SCATTER_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
-                                              sc.bcnt, sc.bitems, sc.bidx, err);
+        kfn<<<grid, PAIR_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
+                                           sc.bcnt, sc.bitems, sc.bidx, err);
     } else {
         auto kfn = k_hash_bucket<SCATTER_THREADS, SCATTER_IPT, false>;
         GQF_CK(set_smem(kfn, sm));
-        kfn<<<grid, SCATTER_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
-                                              sc.bcnt, sc.bitems, nullptr, err);
+        kfn<<<grid, SCATTER_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr,
+                                              exact ? 0xFFFFFFFFu : p.stride, sc.bcnt, sc.bitems, nullptr, err);
     }
     GQF_CK(cudaGetLastError());
     return GQF_OK;

@@ -34,8 +34,13 @@ struct BucketGeom {
     uint32_t fp_mask;       // (1 << (q + r)) - 1
 };
 
-constexpr int SCATTER_THREADS = 512;
-constexpr int SCATTER_IPT = 32;  // 16K keys per CTA
+// Scatter CTA shapes: fingerprints only (build, insert, delete) take 32K
+// keys per CTA, halving the per-(CTA, bucket) global reservations; pairs
+// (sorted lookups) carry an index per key and take 16K.
+constexpr int SCATTER_THREADS = 1024;
+constexpr int SCATTER_IPT = 32;
+constexpr int PAIR_THREADS = 512;
+constexpr int PAIR_IPT = 32;
 constexpr int LAYOUT_THREADS = 512;
 constexpr uint32_t SPILL_SLOTS = 4096;  // tile buffer headroom past the bucket
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
@@ -364,7 +369,8 @@ __host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_it
 {
     size_t S = (size_t)1 << tb;
     size_t r0 = (layout_region0_bytes(tb, cap_items, bpe, bitmap) + 15) & ~(size_t)15;
-    return r0 + (S + SPILL_SLOTS) * bpe + 32;
+    size_t tile = (((S + SPILL_SLOTS) * bpe + 32) + 15) & ~(size_t)15;
+    return r0 + tile + S / 8;  // + occupied bit per quotient
 }
 
 // Group walk (general mode): quotients [qb, qb+QPT) in slot order, calling
@@ -621,16 +627,34 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     const size_t gs = (size_t)lo * BPE;             // first table byte written
     const size_t ge = gs + (size_t)bufslots * BPE;  // end of the buffered part
     const size_t gal = gs & ~(size_t)15;            // smem byte 0 <-> table byte gal
+    // occupied bits of the bucket's own quotients, one bit per slot x0..x0+S
+    uint32_t *s_occ = reinterpret_cast<uint32_t *>(s_tile + (((size_t)BUF * BPE + 32 + 15) & ~(size_t)15));
     for (size_t i = tid * 16; i < ge - gal; i += THREADS * 16)
         *reinterpret_cast<uint4 *>(s_tile + i) = make_uint4(0, 0, 0, 0);
+    for (uint32_t i = tid; i < S / 32; i += THREADS) s_occ[i] = 0;
     __syncthreads();
 
-    // E: emit elements
+    // E: emit elements; record occupied quotients (bit array) and the ones
+    // whose slot an earlier bucket writes (fix-ups)
     {
         uint32_t c = texcl.apply(cin);
         walk([&](uint32_t xa, uint32_t rem, uint32_t kk) {
             uint32_t pos = xa > c ? xa : c;
             c = pos + 1;
+            if (kk == 0) {
+                if (xa >= lo) {
+                    atomicOr(s_occ + ((xa - x0) >> 5), 1u << ((xa - x0) & 31));
+                } else {
+                    uint32_t p = atomicAdd(&s_nfix, 1u);
+                    if (p < 256) {
+                        s_fix[p] = xa;
+                    } else {
+                        uint32_t gp = atomicAdd(a.fix_cnt, 1u);
+                        if (gp < a.fix_cap) a.fix_list[gp] = xa;
+                        else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+                    }
+                }
+            }
             if (pos >= hi) return;  // past the table: reported as FULL
             uint32_t e = (rem << 3) | (kk ? 2u : 0u) | (pos != xa ? 1u : 0u);
             uint8_t *d = (pos - lo < bufslots) ? s_tile + ((size_t)pos * BPE - gal) : a.table + (size_t)pos * BPE;
@@ -643,24 +667,13 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
         });
     }
     __syncthreads();
-    // F: occupied bits (own tile) or fix-ups (slot written by an earlier
-    // bucket); a quotient is occupied iff the rebuilt group is non-empty
-    walk([&](uint32_t xa, uint32_t, uint32_t kk) {
-        if (kk != 0) return;
-        if (xa >= lo) {
-            s_tile[(size_t)xa * BPE + (BPE - 1) - gal] |= 4u;
-        } else {
-            uint32_t p = atomicAdd(&s_nfix, 1u);
-            if (p < 256) {
-                s_fix[p] = xa;
-            } else {
-                uint32_t gp = atomicAdd(a.fix_cnt, 1u);
-                if (gp < a.fix_cap) a.fix_list[gp] = xa;
-                else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
-            }
-        }
-    });
-    __syncthreads();
+    // occupied bit of slot at table byte g (g on an element's last byte)
+    auto occ_at = [&](size_t g) -> uint32_t {
+        size_t slot = g / BPE;
+        if (slot < x0 || slot >= (size_t)x0 + S) return 0u;
+        uint32_t o = (uint32_t)(slot - x0);
+        return (s_occ[o >> 5] >> (o & 31)) & 1u;
+    };
     {
         uint32_t nf = s_nfix < 256 ? s_nfix : 256;
         if (tid == 0 && nf) s_fbase = atomicAdd(a.fix_cnt, nf);
@@ -671,16 +684,41 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
             else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
         }
     }
-    // G: store the tile: head bytes, 16-byte body, tail bytes
+    // G: store the tile (occupied bits merged in): head bytes, 16-byte body,
+    // tail bytes
     {
         size_t h_end = (gs + 15) & ~(size_t)15;
         if (h_end > ge) h_end = ge;
         size_t b_end = ge & ~(size_t)15;
         if (b_end < h_end) b_end = h_end;
-        for (size_t g = gs + tid; g < h_end; g += THREADS) a.table[g] = s_tile[g - gal];
-        for (size_t g = h_end + (size_t)tid * 16; g < b_end; g += (size_t)THREADS * 16)
-            *reinterpret_cast<uint4 *>(a.table + g) = *reinterpret_cast<const uint4 *>(s_tile + (g - gal));
-        for (size_t g = b_end + tid; g < ge; g += THREADS) a.table[g] = s_tile[g - gal];
+        auto byte_out = [&](size_t g) -> uint8_t {
+            uint8_t v = s_tile[g - gal];
+            if ((g % BPE) == BPE - 1) v |= (uint8_t)(occ_at(g) << 2);
+            return v;
+        };
+        for (size_t g = gs + tid; g < h_end; g += THREADS) a.table[g] = byte_out(g);
+        for (size_t g = h_end + (size_t)tid * 16; g < b_end; g += (size_t)THREADS * 16) {
+            uint4 v = *reinterpret_cast<const uint4 *>(s_tile + (g - gal));
+            if (BPE == 1) {
+                // 16 slots: spread their 16 occupied bits onto bit 2 of each byte
+                uint32_t bits = 0;
+                if (g >= x0 && g < (size_t)x0 + S) {  // g - x0 is a multiple of 16
+                    uint32_t o = (uint32_t)(g - x0);
+                    bits = (s_occ[o >> 5] >> (o & 16u)) & 0xFFFFu;
+                }
+                auto spread4 = [](uint32_t x4) -> uint32_t { return ((x4 * 0x00204081u) & 0x01010101u) << 2; };
+                v.x |= spread4(bits & 15u);
+                v.y |= spread4((bits >> 4) & 15u);
+                v.z |= spread4((bits >> 8) & 15u);
+                v.w |= spread4((bits >> 12) & 15u);
+            } else {
+                uint8_t *pb = reinterpret_cast<uint8_t *>(&v);
+                for (int k = 0; k < 16; k++)
+                    if (((g + k) % BPE) == BPE - 1) pb[k] |= (uint8_t)(occ_at(g + k) << 2);
+            }
+            *reinterpret_cast<uint4 *>(a.table + g) = v;
+        }
+        for (size_t g = b_end + tid; g < ge; g += THREADS) a.table[g] = byte_out(g);
     }
 }
 
