@@ -73,11 +73,12 @@ static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_
     int bpe = (r + 3) / 8;
     double avg = (double)n_expect / p.g.nb;
     uint32_t need = (uint32_t)(avg * 1.05 + 10.0 * std::sqrt(avg) + 256.0);
-    p.threads = (1u << tb) >= 1024 ? 512 : 64;
+    // a block needs at least 4 quotients per thread (one uint4 of bitmaps)
+    p.threads = (1u << tb) >= 2048 ? 512 : ((1u << tb) >= 512 ? 128 : 32);
     size_t S = (size_t)1 << tb;
     size_t tile = (((S + SPILL_SLOTS) * bpe + 32 + 15) & ~(size_t)15) + S / 8;
     size_t counters = 4 * (S / 2 + S / 32 + 8);
-    size_t bitmaps = 4 * (S + S / 32 + 8);
+    size_t bitmaps = 4 * S;
     size_t budget = 100 * 1024;
     size_t maxsm = (size_t)(di.smem_optin > 0 ? di.smem_optin : 99 * 1024) - 4096;
     size_t need_bytes = std::max(counters + (size_t)need * bpe, bitmap ? bitmaps : 0) + tile + 16;
@@ -269,10 +270,14 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
         auto k = k_bucket_layout<512, BPE>;
         GQF_CK(set_smem(k, p.smem));
         k<<<p.g.nb, 512, p.smem, s>>>(a);
-    } else {
-        auto k = k_bucket_layout<64, BPE>;
+    } else if (p.threads == 128) {
+        auto k = k_bucket_layout<128, BPE>;
         GQF_CK(set_smem(k, p.smem));
-        k<<<p.g.nb, 64, p.smem, s>>>(a);
+        k<<<p.g.nb, 128, p.smem, s>>>(a);
+    } else {
+        auto k = k_bucket_layout<32, BPE>;
+        GQF_CK(set_smem(k, p.smem));
+        k<<<p.g.nb, 32, p.smem, s>>>(a);
     }
     const DeviceInfo &di = device_info(current_device());
     count_launches(2);

@@ -249,11 +249,10 @@ __device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_
     }
 }
 
-// Shared-memory word skews: a thread that owns a run of consecutive words
-// starts 17 (resp. 33) words after its neighbour, so the lanes of a warp
-// stepping through their runs hit distinct banks.
+// Shared-memory word skew: a thread that owns a run of 16 consecutive words
+// starts 17 words after its neighbour, so the lanes of a warp stepping
+// through their runs hit distinct banks.
 __device__ __forceinline__ uint32_t skew16(uint32_t w) { return w + (w >> 4); }
-__device__ __forceinline__ uint32_t skew32(uint32_t w) { return w + (w >> 5); }
 
 // u16 counters packed two per (skewed) u32 word
 __device__ __forceinline__ uint32_t cnt16_get(const uint32_t *a, uint32_t i)
@@ -362,7 +361,7 @@ __host__ __device__ inline size_t layout_region0_bytes(uint32_t tb, uint32_t cap
 {
     size_t S = (size_t)1 << tb;
     size_t gen = 4 * (S / 2 + S / 32 + 8) + (((size_t)cap_items * bpe + 15) & ~(size_t)15);
-    size_t bit = 4 * (S + S / 32 + 8);
+    size_t bit = 4 * S;
     return bitmap && bit > gen ? bit : gen;
 }
 __host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_items, int bpe, bool bitmap)
@@ -396,22 +395,6 @@ __device__ __forceinline__ void walk_groups(const uint32_t *s_cnt, const Rem *s_
     }
 }
 
-// Bitmap walk: bit v of s_mask[skew32(x)] = remainder v kept at quotient x.
-template <typename Emit>
-__device__ __forceinline__ void walk_bits(const uint32_t *s_mask, uint32_t qb, uint32_t QPT, uint32_t x0, Emit &&emit)
-{
-    for (uint32_t j = 0; j < QPT; j++) {
-        uint32_t x = qb + j;
-        uint32_t m = s_mask[skew32(x)];
-        uint32_t kk = 0;
-        while (m) {
-            uint32_t v = (uint32_t)__ffs(m) - 1u;
-            m &= m - 1u;
-            emit(x0 + x, v, kk++);
-        }
-    }
-}
-
 // ---------------------------------------------------------------------
 // K2: one CTA per bucket (taken in ticket order for the look-back).
 // ---------------------------------------------------------------------
@@ -423,7 +406,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     const uint32_t S = 1u << a.tb;
     const bool bitmap = BPE == 1 && a.bitmap_ok && !(a.a_dups && *a.a_dups);
     uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem_layout);   // general: u16 counters
-    uint32_t *s_mask = reinterpret_cast<uint32_t *>(smem_layout);  // bitmap: u32 per quotient
+    uint32_t *s_mask = reinterpret_cast<uint32_t *>(smem_layout);  // bitmap: u32 per local quotient
     Rem *s_rem = reinterpret_cast<Rem *>(smem_layout + 4 * ((size_t)S / 2 + S / 32 + 8));
     uint8_t *s_tile = smem_layout + ((layout_region0_bytes(a.tb, a.cap_items, BPE, a.bitmap_ok != 0) + 15) &
                                      ~(size_t)15);
@@ -447,7 +430,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     const size_t abase = na ? a.A.start(b) : 0, bbase = nbn ? a.B.start(b) : 0;
     const uint32_t x0 = b * S;  // first quotient of the bucket
     const uint32_t rmask = (1u << a.r) - 1u;
-    const uint32_t QPT = S / THREADS;  // S >= 2 * THREADS, power of two
+    const uint32_t QPT = S / THREADS;  // S >= 4 * THREADS, power of two
     const uint32_t qb = tid * QPT;
 
     if (!bitmap && n > a.cap_items) {
@@ -466,7 +449,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
 
     if (bitmap) {
         // A: remainder sets by quotient (A first, then B)
-        for (uint32_t i = tid; i < S + S / 32 + 8; i += THREADS) s_mask[i] = 0;
+        for (uint32_t i = tid; i < S / 4; i += THREADS) reinterpret_cast<uint4 *>(s_mask)[i] = make_uint4(0, 0, 0, 0);
         __syncthreads();
         for (int src = 0; src < 2; src++) {
             const uint32_t lo_i = src ? na : 0u, hi_i = src ? n : na;
@@ -481,7 +464,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
 #pragma unroll
                 for (int k = 0; k < LB; k++) {
                     if (i0 + k * THREADS + tid < hi_i) {
-                        uint32_t w = skew32((v[k] >> a.r) & (S - 1)), bit = 1u << (v[k] & rmask);
+                        uint32_t w = (v[k] >> a.r) & (S - 1), bit = 1u << (v[k] & rmask);
                         if (clear) atomicAnd(s_mask + w, ~bit);
                         else atomicOr(s_mask + w, bit);
                     }
@@ -560,38 +543,68 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
             if (g1 - g0 > 1) small_sort(s_rem + g0, g1 - g0);
         }
     }
-    // every item the rebuilt bucket keeps, in slot order, for this thread
-    auto walk = [&](auto &&emit) {
-        if (bitmap) walk_bits(s_mask, qb, QPT, x0, emit);
-        else walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, emit);
-    };
-
-    // B: this thread's layout map (slot recurrence from slot 0)
-    LayoutFn fn{0u, 0u};
-    {
-        uint32_t c = 0, cnt_items = 0;
-        walk([&](uint32_t xa, uint32_t, uint32_t) {
-            uint32_t pos = xa > c ? xa : c;
-            c = pos + 1;
-            cnt_items++;
-        });
-        fn.n = cnt_items;
-        fn.F = cnt_items ? c : 0u;
-    }
-    // C: block scan of layout maps (exclusive per thread + bucket total)
-    LayoutFn incl = fn;
+    // Bitmap mode: warp w owns quotients [w*QW, (w+1)*QW); a round covers
+    // 128 of them, lane l taking 4 consecutive ones (one uint4 of masks).
+    // The layout maps of a round are combined with a warp shuffle scan.
+    const uint32_t QW = S / (THREADS / 32);
+    const uint32_t ROUNDS = QW / 128;
+    auto round_fn = [&](uint32_t r, uint4 &m4) -> LayoutFn {
+        const uint32_t lq = wid * QW + r * 128 + 4 * lane;  // local quotient of m4.x
+        m4 = reinterpret_cast<const uint4 *>(s_mask)[lq >> 2];
+        const uint32_t mm[4] = {m4.x, m4.y, m4.z, m4.w};
+        LayoutFn f{0u, 0u};
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        LayoutFn p;
-        p.n = __shfl_up_sync(0xffffffffu, incl.n, o);
-        p.F = __shfl_up_sync(0xffffffffu, incl.F, o);
-        if (lane >= o) incl = compose(p, incl);
+        for (int k = 0; k < 4; k++) {
+            uint32_t c = __popc(mm[k]);
+            if (c) f = compose(f, LayoutFn{c, x0 + lq + k + c});
+        }
+        return f;
+    };
+    auto warp_incl = [&](LayoutFn f) -> LayoutFn {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            LayoutFn p;
+            p.n = __shfl_up_sync(0xffffffffu, f.n, o);
+            p.F = __shfl_up_sync(0xffffffffu, f.F, o);
+            if (lane >= o) f = compose(p, f);
+        }
+        return f;
+    };
+    // every item the rebuilt bucket keeps, in slot order, for this thread
+    // (general mode)
+    auto walk = [&](auto &&emit) { walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, emit); };
+
+    // B/C: layout maps -- per warp (bitmap) or per thread then per warp
+    LayoutFn wexcl{0u, 0u};
+    if (bitmap) {
+        LayoutFn wacc{0u, 0u};
+        for (uint32_t r = 0; r < ROUNDS; r++) {
+            uint4 m4;
+            LayoutFn incl = warp_incl(round_fn(r, m4));
+            LayoutFn tot;
+            tot.n = __shfl_sync(0xffffffffu, incl.n, 31);
+            tot.F = __shfl_sync(0xffffffffu, incl.F, 31);
+            wacc = compose(wacc, tot);
+        }
+        if (lane == 0) s_wfn[wid] = wacc;
+    } else {
+        LayoutFn fn{0u, 0u};
+        {
+            uint32_t c = 0, cnt_items = 0;
+            walk([&](uint32_t xa, uint32_t, uint32_t) {
+                uint32_t pos = xa > c ? xa : c;
+                c = pos + 1;
+                cnt_items++;
+            });
+            fn.n = cnt_items;
+            fn.F = cnt_items ? c : 0u;
+        }
+        LayoutFn incl = warp_incl(fn);
+        wexcl.n = __shfl_up_sync(0xffffffffu, incl.n, 1);
+        wexcl.F = __shfl_up_sync(0xffffffffu, incl.F, 1);
+        if (lane == 0) wexcl = LayoutFn{0u, 0u};
+        if (lane == 31) s_wfn[wid] = incl;
     }
-    LayoutFn wexcl;
-    wexcl.n = __shfl_up_sync(0xffffffffu, incl.n, 1);
-    wexcl.F = __shfl_up_sync(0xffffffffu, incl.F, 1);
-    if (lane == 0) wexcl = LayoutFn{0u, 0u};
-    if (lane == 31) s_wfn[wid] = incl;
     __syncthreads();
     if (wid == 0) {
         LayoutFn acc{0u, 0u};
@@ -615,7 +628,6 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     }
     __syncthreads();
     const uint32_t cin = s_cin, cout = s_cout;
-    const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
     const uint32_t lo = cin > x0 ? cin : x0;
     uint32_t hi = cout > x0 + S ? cout : x0 + S;
     if (hi > a.nslots) {
@@ -634,36 +646,80 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     for (uint32_t i = tid; i < S / 32; i += THREADS) s_occ[i] = 0;
     __syncthreads();
 
+    auto put_elem = [&](uint32_t pos, uint32_t e) {
+        uint8_t *d = (pos - lo < bufslots) ? s_tile + ((size_t)pos * BPE - gal) : a.table + (size_t)pos * BPE;
+        if (BPE == 1) {
+            d[0] = (uint8_t)e;
+        } else {
+            d[0] = (uint8_t)(e >> 8);
+            d[1] = (uint8_t)e;
+        }
+    };
+    auto add_fix = [&](uint32_t xa) {
+        uint32_t p = atomicAdd(&s_nfix, 1u);
+        if (p < 256) {
+            s_fix[p] = xa;
+        } else {
+            uint32_t gp = atomicAdd(a.fix_cnt, 1u);
+            if (gp < a.fix_cap) a.fix_list[gp] = xa;
+            else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+        }
+    };
     // E: emit elements; record occupied quotients (bit array) and the ones
     // whose slot an earlier bucket writes (fix-ups)
-    {
+    if (bitmap) {
+        uint32_t c = s_wexcl[wid].apply(cin);  // entry slot of this warp's quotients
+        for (uint32_t r = 0; r < ROUNDS; r++) {
+            uint4 m4;
+            LayoutFn incl = warp_incl(round_fn(r, m4));
+            LayoutFn ex;
+            ex.n = __shfl_up_sync(0xffffffffu, incl.n, 1);
+            ex.F = __shfl_up_sync(0xffffffffu, incl.F, 1);
+            if (lane == 0) ex = LayoutFn{0u, 0u};
+            LayoutFn tot;
+            tot.n = __shfl_sync(0xffffffffu, incl.n, 31);
+            tot.F = __shfl_sync(0xffffffffu, incl.F, 31);
+            const uint32_t lq = wid * QW + r * 128 + 4 * lane;
+            const uint32_t mm[4] = {m4.x, m4.y, m4.z, m4.w};
+            uint32_t cl = ex.apply(c), nib = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                uint32_t m = mm[k];
+                if (!m) continue;
+                const uint32_t xa = x0 + lq + k;
+                const uint32_t start = xa > cl ? xa : cl;
+                uint32_t pos = start, kk = 0;
+                while (m) {
+                    uint32_t v = (uint32_t)__ffs(m) - 1u;
+                    m &= m - 1u;
+                    if (pos < hi) put_elem(pos, (v << 3) | (kk ? 2u : 0u) | (pos != xa ? 1u : 0u));
+                    pos++;
+                    kk++;
+                }
+                cl = pos;
+                if (xa >= lo) nib |= 1u << k;
+                else add_fix(xa);
+            }
+            // occupied bits: 8 lanes x 4 quotients = one 32-bit word
+            uint32_t w = nib << (4 * (lane & 7));
+            w |= __shfl_xor_sync(0xffffffffu, w, 1);
+            w |= __shfl_xor_sync(0xffffffffu, w, 2);
+            w |= __shfl_xor_sync(0xffffffffu, w, 4);
+            if ((lane & 7) == 0) s_occ[lq >> 5] = w;
+            c = tot.apply(c);
+        }
+    } else {
+        const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
         uint32_t c = texcl.apply(cin);
         walk([&](uint32_t xa, uint32_t rem, uint32_t kk) {
             uint32_t pos = xa > c ? xa : c;
             c = pos + 1;
             if (kk == 0) {
-                if (xa >= lo) {
-                    atomicOr(s_occ + ((xa - x0) >> 5), 1u << ((xa - x0) & 31));
-                } else {
-                    uint32_t p = atomicAdd(&s_nfix, 1u);
-                    if (p < 256) {
-                        s_fix[p] = xa;
-                    } else {
-                        uint32_t gp = atomicAdd(a.fix_cnt, 1u);
-                        if (gp < a.fix_cap) a.fix_list[gp] = xa;
-                        else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
-                    }
-                }
+                if (xa >= lo) atomicOr(s_occ + ((xa - x0) >> 5), 1u << ((xa - x0) & 31));
+                else add_fix(xa);
             }
             if (pos >= hi) return;  // past the table: reported as FULL
-            uint32_t e = (rem << 3) | (kk ? 2u : 0u) | (pos != xa ? 1u : 0u);
-            uint8_t *d = (pos - lo < bufslots) ? s_tile + ((size_t)pos * BPE - gal) : a.table + (size_t)pos * BPE;
-            if (BPE == 1) {
-                d[0] = (uint8_t)e;
-            } else {
-                d[0] = (uint8_t)(e >> 8);
-                d[1] = (uint8_t)e;
-            }
+            put_elem(pos, (rem << 3) | (kk ? 2u : 0u) | (pos != xa ? 1u : 0u));
         });
     }
     __syncthreads();
