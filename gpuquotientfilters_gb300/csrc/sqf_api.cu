@@ -73,12 +73,11 @@ static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_
     int bpe = (r + 3) / 8;
     double avg = (double)n_expect / p.g.nb;
     uint32_t need = (uint32_t)(avg * 1.05 + 10.0 * std::sqrt(avg) + 256.0);
-    // a block needs at least 4 quotients per thread (one uint4 of bitmaps)
-    p.threads = (1u << tb) >= 2048 ? 512 : ((1u << tb) >= 512 ? 128 : 32);
+    p.threads = tb >= 10 ? (1 << (tb - 5)) : 32;
     size_t S = (size_t)1 << tb;
     size_t tile = (((S + SPILL_SLOTS) * bpe + 32 + 15) & ~(size_t)15) + S / 8;
     size_t counters = 4 * (S / 2 + S / 32 + 8);
-    size_t bitmaps = 4 * S;
+    size_t bitmaps = 4 * (S + S / 8);
     size_t budget = 100 * 1024;
     size_t maxsm = (size_t)(di.smem_optin > 0 ? di.smem_optin : 99 * 1024) - 4096;
     size_t need_bytes = std::max(counters + (size_t)need * bpe, bitmap ? bitmaps : 0) + tile + 16;
@@ -266,19 +265,25 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
     a.fix_cnt = sc.fix_cnt;
     a.fix_cap = sc.fix_cap;
     a.err = err;
-    if (p.threads == 512) {
-        auto k = k_bucket_layout<512, BPE>;
-        GQF_CK(set_smem(k, p.smem));
-        k<<<p.g.nb, 512, p.smem, s>>>(a);
-    } else if (p.threads == 128) {
-        auto k = k_bucket_layout<128, BPE>;
-        GQF_CK(set_smem(k, p.smem));
-        k<<<p.g.nb, 128, p.smem, s>>>(a);
-    } else {
-        auto k = k_bucket_layout<32, BPE>;
-        GQF_CK(set_smem(k, p.smem));
-        k<<<p.g.nb, 32, p.smem, s>>>(a);
+    // one thread per 32 consecutive quotients (fewer per thread below 1024
+    // quotients per bucket)
+    cudaError_t e = cudaSuccess;
+    auto go = [&](auto kernel, int threads) {
+        e = set_smem(kernel, p.smem);
+        if (e == cudaSuccess) kernel<<<p.g.nb, threads, p.smem, s>>>(a);
+    };
+    switch (p.g.tb) {
+    case 15: go(k_bucket_layout<1024, 32, BPE>, 1024); break;
+    case 14: go(k_bucket_layout<512, 32, BPE>, 512); break;
+    case 13: go(k_bucket_layout<256, 32, BPE>, 256); break;
+    case 12: go(k_bucket_layout<128, 32, BPE>, 128); break;
+    case 11: go(k_bucket_layout<64, 32, BPE>, 64); break;
+    case 10: go(k_bucket_layout<32, 32, BPE>, 32); break;
+    case 9: go(k_bucket_layout<32, 16, BPE>, 32); break;
+    case 8: go(k_bucket_layout<32, 8, BPE>, 32); break;
+    default: go(k_bucket_layout<32, 4, BPE>, 32); break;
     }
+    GQF_CK(e);
     const DeviceInfo &di = device_info(current_device());
     count_launches(2);
     k_fixup_occ<BPE><<<di.sms * 2, 256, 0, s>>>(table, sc.fix_list, sc.fix_cnt, sc.fix_cap);

@@ -254,6 +254,15 @@ __device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_
 // through their runs hit distinct banks.
 __device__ __forceinline__ uint32_t skew16(uint32_t w) { return w + (w >> 4); }
 
+// Bitmap layout: one u32 remainder set per local quotient, one pad uint4
+// after every 8 uint4s, so threads owning 32 consecutive quotients sit 9
+// uint4s apart and a quarter-warp of uint4 loads covers all 32 banks.
+__device__ __forceinline__ uint32_t mask_word(uint32_t x)
+{
+    uint32_t u = x >> 2;
+    return 4 * (u + (u >> 3)) + (x & 3u);
+}
+
 // u16 counters packed two per (skewed) u32 word
 __device__ __forceinline__ uint32_t cnt16_get(const uint32_t *a, uint32_t i)
 {
@@ -361,7 +370,7 @@ __host__ __device__ inline size_t layout_region0_bytes(uint32_t tb, uint32_t cap
 {
     size_t S = (size_t)1 << tb;
     size_t gen = 4 * (S / 2 + S / 32 + 8) + (((size_t)cap_items * bpe + 15) & ~(size_t)15);
-    size_t bit = 4 * S;
+    size_t bit = 4 * (S + S / 8);
     return bitmap && bit > gen ? bit : gen;
 }
 __host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_items, int bpe, bool bitmap)
@@ -398,8 +407,9 @@ __device__ __forceinline__ void walk_groups(const uint32_t *s_cnt, const Rem *s_
 // ---------------------------------------------------------------------
 // K2: one CTA per bucket (taken in ticket order for the look-back).
 // ---------------------------------------------------------------------
-template <int THREADS, int BPE>
-__global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
+// THREADS threads own QPT consecutive quotients each (S = THREADS * QPT).
+template <int THREADS, int QPT_, int BPE>
+__global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_layout(LayoutArgs a)
 {
     using Rem = typename std::conditional<BPE == 1, uint8_t, uint16_t>::type;
     extern __shared__ __align__(16) uint8_t smem_layout[];
@@ -430,7 +440,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     const size_t abase = na ? a.A.start(b) : 0, bbase = nbn ? a.B.start(b) : 0;
     const uint32_t x0 = b * S;  // first quotient of the bucket
     const uint32_t rmask = (1u << a.r) - 1u;
-    const uint32_t QPT = S / THREADS;  // S >= 4 * THREADS, power of two
+    constexpr uint32_t QPT = QPT_;  // S == THREADS * QPT
     const uint32_t qb = tid * QPT;
 
     if (!bitmap && n > a.cap_items) {
@@ -448,8 +458,10 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     constexpr int LB = 8;
 
     if (bitmap) {
-        // A: remainder sets by quotient (A first, then B)
-        for (uint32_t i = tid; i < S / 4; i += THREADS) reinterpret_cast<uint4 *>(s_mask)[i] = make_uint4(0, 0, 0, 0);
+        // A: remainder sets by quotient (A first, then B); mask of local
+        // quotient x lives at word mask_word(x) (one pad uint4 per 8)
+        for (uint32_t i = tid; i < (S + S / 8) / 4; i += THREADS)
+            reinterpret_cast<uint4 *>(s_mask)[i] = make_uint4(0, 0, 0, 0);
         __syncthreads();
         for (int src = 0; src < 2; src++) {
             const uint32_t lo_i = src ? na : 0u, hi_i = src ? n : na;
@@ -464,7 +476,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
 #pragma unroll
                 for (int k = 0; k < LB; k++) {
                     if (i0 + k * THREADS + tid < hi_i) {
-                        uint32_t w = (v[k] >> a.r) & (S - 1), bit = 1u << (v[k] & rmask);
+                        uint32_t w = mask_word((v[k] >> a.r) & (S - 1)), bit = 1u << (v[k] & rmask);
                         if (clear) atomicAnd(s_mask + w, ~bit);
                         else atomicOr(s_mask + w, bit);
                     }
@@ -543,23 +555,19 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
             if (g1 - g0 > 1) small_sort(s_rem + g0, g1 - g0);
         }
     }
-    // Bitmap mode: warp w owns quotients [w*QW, (w+1)*QW); a round covers
-    // 128 of them, lane l taking 4 consecutive ones (one uint4 of masks).
-    // The layout maps of a round are combined with a warp shuffle scan.
-    const uint32_t QW = S / (THREADS / 32);
-    const uint32_t ROUNDS = QW / 128;
-    auto round_fn = [&](uint32_t r, uint4 &m4) -> LayoutFn {
-        const uint32_t lq = wid * QW + r * 128 + 4 * lane;  // local quotient of m4.x
-        m4 = reinterpret_cast<const uint4 *>(s_mask)[lq >> 2];
-        const uint32_t mm[4] = {m4.x, m4.y, m4.z, m4.w};
-        LayoutFn f{0u, 0u};
+    // Bitmap mode: this thread's QPT remainder sets, held in registers
+    // (QPT/4 conflict-free uint4 loads: thread strides are 9 uint4 apart).
+    uint32_t mreg[QPT];
+    if (bitmap) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            uint32_t c = __popc(mm[k]);
-            if (c) f = compose(f, LayoutFn{c, x0 + lq + k + c});
+        for (uint32_t j = 0; j < QPT / 4; j++) {
+            uint4 m4 = reinterpret_cast<const uint4 *>(s_mask)[mask_word(qb + 4 * j) >> 2];
+            mreg[4 * j] = m4.x;
+            mreg[4 * j + 1] = m4.y;
+            mreg[4 * j + 2] = m4.z;
+            mreg[4 * j + 3] = m4.w;
         }
-        return f;
-    };
+    }
     auto warp_incl = [&](LayoutFn f) -> LayoutFn {
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -574,31 +582,33 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     // (general mode)
     auto walk = [&](auto &&emit) { walk_groups(s_cnt, s_rem, qb, QPT, x0, a.op, a.nodup, emit); };
 
-    // B/C: layout maps -- per warp (bitmap) or per thread then per warp
-    LayoutFn wexcl{0u, 0u};
+    // B/C: this thread's layout map, then a warp scan of the maps
+    LayoutFn fn{0u, 0u};
     if (bitmap) {
-        LayoutFn wacc{0u, 0u};
-        for (uint32_t r = 0; r < ROUNDS; r++) {
-            uint4 m4;
-            LayoutFn incl = warp_incl(round_fn(r, m4));
-            LayoutFn tot;
-            tot.n = __shfl_sync(0xffffffffu, incl.n, 31);
-            tot.F = __shfl_sync(0xffffffffu, incl.F, 31);
-            wacc = compose(wacc, tot);
+        uint32_t c = 0, cnt_items = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < QPT; j++) {
+            uint32_t k = __popc(mreg[j]);
+            if (k) {
+                uint32_t xa = x0 + qb + j;
+                c = (xa > c ? xa : c) + k;
+                cnt_items += k;
+            }
         }
-        if (lane == 0) s_wfn[wid] = wacc;
+        fn.n = cnt_items;
+        fn.F = cnt_items ? c : 0u;
     } else {
-        LayoutFn fn{0u, 0u};
-        {
-            uint32_t c = 0, cnt_items = 0;
-            walk([&](uint32_t xa, uint32_t, uint32_t) {
-                uint32_t pos = xa > c ? xa : c;
-                c = pos + 1;
-                cnt_items++;
-            });
-            fn.n = cnt_items;
-            fn.F = cnt_items ? c : 0u;
-        }
+        uint32_t c = 0, cnt_items = 0;
+        walk([&](uint32_t xa, uint32_t, uint32_t) {
+            uint32_t pos = xa > c ? xa : c;
+            c = pos + 1;
+            cnt_items++;
+        });
+        fn.n = cnt_items;
+        fn.F = cnt_items ? c : 0u;
+    }
+    LayoutFn wexcl{0u, 0u};
+    {
         LayoutFn incl = warp_incl(fn);
         wexcl.n = __shfl_up_sync(0xffffffffu, incl.n, 1);
         wexcl.F = __shfl_up_sync(0xffffffffu, incl.F, 1);
@@ -668,46 +678,34 @@ __global__ void __launch_bounds__(THREADS, 2) k_bucket_layout(LayoutArgs a)
     // E: emit elements; record occupied quotients (bit array) and the ones
     // whose slot an earlier bucket writes (fix-ups)
     if (bitmap) {
-        uint32_t c = s_wexcl[wid].apply(cin);  // entry slot of this warp's quotients
-        for (uint32_t r = 0; r < ROUNDS; r++) {
-            uint4 m4;
-            LayoutFn incl = warp_incl(round_fn(r, m4));
-            LayoutFn ex;
-            ex.n = __shfl_up_sync(0xffffffffu, incl.n, 1);
-            ex.F = __shfl_up_sync(0xffffffffu, incl.F, 1);
-            if (lane == 0) ex = LayoutFn{0u, 0u};
-            LayoutFn tot;
-            tot.n = __shfl_sync(0xffffffffu, incl.n, 31);
-            tot.F = __shfl_sync(0xffffffffu, incl.F, 31);
-            const uint32_t lq = wid * QW + r * 128 + 4 * lane;
-            const uint32_t mm[4] = {m4.x, m4.y, m4.z, m4.w};
-            uint32_t cl = ex.apply(c), nib = 0;
+        const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
+        uint32_t c = texcl.apply(cin);
+        uint32_t occ = 0;  // bit j: quotient qb + j occupied (and in this tile)
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                uint32_t m = mm[k];
-                if (!m) continue;
-                const uint32_t xa = x0 + lq + k;
-                const uint32_t start = xa > cl ? xa : cl;
-                uint32_t pos = start, kk = 0;
-                while (m) {
-                    uint32_t v = (uint32_t)__ffs(m) - 1u;
-                    m &= m - 1u;
-                    if (pos < hi) put_elem(pos, (v << 3) | (kk ? 2u : 0u) | (pos != xa ? 1u : 0u));
-                    pos++;
-                    kk++;
-                }
-                cl = pos;
-                if (xa >= lo) nib |= 1u << k;
-                else add_fix(xa);
+        for (uint32_t j = 0; j < QPT; j++) {
+            uint32_t m = mreg[j];
+            if (!m) continue;
+            const uint32_t xa = x0 + qb + j;
+            uint32_t pos = xa > c ? xa : c;
+            if (xa >= lo) occ |= 1u << (j & 31);
+            else add_fix(xa);
+            uint32_t e0 = pos != xa ? 1u : 0u;  // shifted
+            do {
+                uint32_t v = (uint32_t)__ffs(m) - 1u;
+                m &= m - 1u;
+                if (pos < hi) put_elem(pos, (v << 3) | e0);
+                e0 = 3u;  // later items: continuation + shifted
+                pos++;
+            } while (m);
+            c = pos;
+            if ((j & 31) == 31 || j == QPT - 1) {
+                uint32_t o = (qb + j) & ~31u;  // local quotient of bit 0
+                if (QPT >= 32) s_occ[o >> 5] = occ;
+                else if (occ) atomicOr(s_occ + (o >> 5), occ << ((qb & 31) & ~(QPT - 1)));
+                occ = 0;
             }
-            // occupied bits: 8 lanes x 4 quotients = one 32-bit word
-            uint32_t w = nib << (4 * (lane & 7));
-            w |= __shfl_xor_sync(0xffffffffu, w, 1);
-            w |= __shfl_xor_sync(0xffffffffu, w, 2);
-            w |= __shfl_xor_sync(0xffffffffu, w, 4);
-            if ((lane & 7) == 0) s_occ[lq >> 5] = w;
-            c = tot.apply(c);
         }
+        if (QPT < 32 && occ) atomicOr(s_occ + (qb >> 5), occ << (qb & 31));
     } else {
         const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
         uint32_t c = texcl.apply(cin);
