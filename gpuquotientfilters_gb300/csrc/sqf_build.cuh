@@ -684,28 +684,27 @@ __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_l
 #pragma unroll
         for (uint32_t j = 0; j < QPT; j++) {
             uint32_t m = mreg[j];
-            if (!m) continue;
-            const uint32_t xa = x0 + qb + j;
-            uint32_t pos = xa > c ? xa : c;
-            if (xa >= lo) occ |= 1u << (j & 31);
-            else add_fix(xa);
-            uint32_t e0 = pos != xa ? 1u : 0u;  // shifted
-            do {
-                uint32_t v = (uint32_t)__ffs(m) - 1u;
-                m &= m - 1u;
-                if (pos < hi) put_elem(pos, (v << 3) | e0);
-                e0 = 3u;  // later items: continuation + shifted
-                pos++;
-            } while (m);
-            c = pos;
-            if ((j & 31) == 31 || j == QPT - 1) {
-                uint32_t o = (qb + j) & ~31u;  // local quotient of bit 0
-                if (QPT >= 32) s_occ[o >> 5] = occ;
-                else if (occ) atomicOr(s_occ + (o >> 5), occ << ((qb & 31) & ~(QPT - 1)));
+            if (m) {
+                const uint32_t xa = x0 + qb + j;
+                uint32_t pos = xa > c ? xa : c;
+                if (xa >= lo) occ |= 1u << (j & 31);
+                else add_fix(xa);
+                uint32_t e0 = pos != xa ? 1u : 0u;  // shifted
+                do {
+                    uint32_t v = (uint32_t)__ffs(m) - 1u;
+                    m &= m - 1u;
+                    if (pos < hi) put_elem(pos, (v << 3) | e0);
+                    e0 = 3u;  // later items: continuation + shifted
+                    pos++;
+                } while (m);
+                c = pos;
+            }
+            if (QPT >= 32 && (j & 31) == 31) {
+                s_occ[(qb + j) >> 5] = occ;  // this thread owns the whole word
                 occ = 0;
             }
         }
-        if (QPT < 32 && occ) atomicOr(s_occ + (qb >> 5), occ << (qb & 31));
+        if (QPT < 32 && occ) atomicOr(s_occ + (qb >> 5), occ << (qb & 31));  // shared word
     } else {
         const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
         uint32_t c = texcl.apply(cin);
