@@ -22,7 +22,8 @@ NOT_FOUND = 0xFFFFFFFF
 RBITS = 5
 SLOTS_PER_BLOCK = 64
 
-GQF_OK, GQF_ERR_ARG, GQF_ERR_FULL, GQF_ERR_CUDA, GQF_ERR_TIMEOUT, GQF_ERR_NOMEM, GQF_ERR_MISMATCH = range(7)
+(GQF_OK, GQF_ERR_ARG, GQF_ERR_FULL, GQF_ERR_CUDA, GQF_ERR_TIMEOUT, GQF_ERR_NOMEM, GQF_ERR_MISMATCH,
+ GQF_ERR_LIMIT) = range(8)
 
 
 class GQFError(RuntimeError):
@@ -77,6 +78,8 @@ def _lib():
             "gqf_sqf_delete": (i32, [qfp, i32, vp, vp, f32p]),
             "gqf_sqf_insert_via_merge": (i32, [qfp, vp, i32, vp, i32, i32, vp, f32p]),
             "gqf_sqf_merge": (i32, [qfp, qfp, i32, vp, f32p]),
+            "gqf_sqf_bulk_build_noalloc": (i32, [qfp, i32, vp, i32, vp]),
+            "gqf_kernel_launches": (C.c_ulonglong, []),
             "gqf_rsqf_init": (i32, [cqfp, C.c_uint]),
             "gqf_rsqf_free": (i32, [cqfp]),
             "gqf_rsqf_insert": (i32, [cqfp, i32, vp, vp, vp, f32p]),

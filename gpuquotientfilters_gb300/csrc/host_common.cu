@@ -127,6 +127,7 @@ const char *gqf_status_string(int st)
     case GQF_ERR_TIMEOUT: return "device wait timed out";
     case GQF_ERR_NOMEM: return "workspace allocation failed";
     case GQF_ERR_MISMATCH: return "filters differ in q or r";
+    case GQF_ERR_LIMIT: return "request exceeds the no-allocation entry point's fixed scratch (see GQF_NOALLOC_MAX_KEYS, GQF_NOALLOC_MAX_Q)";
     default: return "unknown status";
     }
 }

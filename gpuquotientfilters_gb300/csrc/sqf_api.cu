@@ -420,6 +420,54 @@ static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint3
     return call_end(ar, s, ms);
 }
 
+
+// ------------------------------------------------ no-allocation bulk build
+// Scratch for gqf_sqf_bulk_build_noalloc: a fixed array in the library's
+// device image.  Host code must not use the symbol itself as an address;
+// each device's address comes from cudaGetSymbolAddress on that device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GQF_NOALLOC_SCRATCH_BYTES];
+static void *g_noalloc_base[64];
+static std::mutex g_noalloc_mu;
+
+template <int BPE>
+static int bulk_build_noalloc_t(const gqf_sqf *qf, uint32_t n, const uint32_t *keys, int nodup, cudaStream_t s)
+{
+    const int dev = current_device();
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_base[dev & 63]) {
+        void *ptr = nullptr;
+        GQF_CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        g_noalloc_base[dev & 63] = ptr;
+    }
+    char *base = static_cast<char *>(g_noalloc_base[dev & 63]);
+    const SqfGeom tg = geom_of(qf);
+    const bool bitmap_ok = tg.r == 5 && nodup;
+    LayoutPlan p = plan_layout(tg.q, tg.r, n, n, bitmap_ok);
+    ScratchReq req{p.g.nb, std::max<size_t>(n, 1), false, false, false, tg.nslots};
+    size_t need = 0;
+    carve(nullptr, req, true, &need);
+    const size_t err_off = GQF_NOALLOC_SCRATCH_BYTES - 256;  // device error word
+    if (need > err_off) return GQF_ERR_LIMIT;
+    size_t got = 0;
+    Scratch sc = carve(base, req, false, &got);
+    uint32_t *err = reinterpret_cast<uint32_t *>(base + err_off);
+    // the array keeps the previous call's contents: clear what starts at zero
+    GQF_CK(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
+    GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
+    BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
+    if (n) {
+        int st = bucket_batch(keys, n, p, sc, true, false, err, s);
+        if (st) return st;
+        B = BucketSrc{sc.bitems, sc.bbase, 0, sc.bcnt};
+    }
+    int st = launch_layout<BPE>(p, tg, qf->table, A, B, OP_BUILD, nodup, bitmap_ok, nullptr, sc, err, s);
+    if (st) return st;
+    GQF_CK(cudaStreamSynchronize(s));
+    uint32_t e = 0;
+    GQF_CK(cudaMemcpy(&e, err, sizeof(e), cudaMemcpyDeviceToHost));
+    return dev_err_to_status(e);
+}
+
 }  // namespace gqf
 
 using namespace gqf;
@@ -467,6 +515,14 @@ int gqf_sqf_bulk_build(const gqf_sqf *qf, int n, const uint32_t *d_keys, int no_
     if (!sqf_ok(qf) || n < 0 || (n > 0 && !d_keys)) return GQF_ERR_ARG;
     return BPE_DISPATCH(qf, rebuild, qf, nullptr, d_keys, (uint32_t)n, OP_BUILD, no_duplicates ? 1 : 0,
                         static_cast<cudaStream_t>(stream), ms);
+}
+
+int gqf_sqf_bulk_build_noalloc(const gqf_sqf *qf, int n, const uint32_t *d_keys, int no_duplicates, void *stream)
+{
+    if (!sqf_ok(qf) || n < 0 || (n > 0 && !d_keys)) return GQF_ERR_ARG;
+    if ((unsigned)n > GQF_NOALLOC_MAX_KEYS || qf->qbits > GQF_NOALLOC_MAX_Q) return GQF_ERR_LIMIT;
+    return BPE_DISPATCH(qf, bulk_build_noalloc_t, qf, (uint32_t)n, d_keys, no_duplicates ? 1 : 0,
+                        static_cast<cudaStream_t>(stream));
 }
 
 int gqf_sqf_insert(const gqf_sqf *qf, int n, const uint32_t *d_keys, void *stream, float *ms)

@@ -30,7 +30,8 @@ typedef enum gqf_status {
     GQF_ERR_CUDA = 3,      /* a CUDA runtime call failed                    */
     GQF_ERR_TIMEOUT = 4,   /* a bounded device-side wait ran out            */
     GQF_ERR_NOMEM = 5,     /* workspace allocation failed                   */
-    GQF_ERR_MISMATCH = 6   /* mergeTwoFilters on filters of different q/r   */
+    GQF_ERR_MISMATCH = 6,  /* mergeTwoFilters on filters of different q/r   */
+    GQF_ERR_LIMIT = 7      /* request larger than the fixed no-allocation scratch */
 } gqf_status;
 
 /* Standard quotient filter handle: identical to `struct quotient_filter`
@@ -117,6 +118,27 @@ int gqf_sqf_insert_via_merge(const gqf_sqf *qf, const uint32_t *d_old, int n_old
 /* mergeTwoFilters, quotientFilter.cu:1744-1891: qf1 := qf1 + qf2. */
 int gqf_sqf_merge(const gqf_sqf *qf1, const gqf_sqf *qf2, int no_duplicates,
                   void *stream, float *ms);
+
+/* Bulk build that allocates no device memory (no counterpart in the
+ * reference).  It is for callers that cannot call cudaMalloc while they run:
+ * a process whose own pool allocator reserved the GPU's memory at start-up,
+ * a latency-critical stream where cudaMalloc/cudaFree's implicit device
+ * synchronisation would stall other streams, or a service with a fixed
+ * memory budget that must not grow after start-up.  The caller still owns
+ * the filter table and the keys.  Scratch is a fixed array in the library's
+ * device image (GQF_NOALLOC_SCRATCH_BYTES per GPU that loads the library,
+ * held until the process exits); requests beyond GQF_NOALLOC_MAX_KEYS keys
+ * or GQF_NOALLOC_MAX_Q quotient bits return GQF_ERR_LIMIT.  The first call
+ * on a device looks up the array's device address, so make that first call
+ * before any stream capture.  Every call shares the one array: calls whose
+ * work overlaps on the GPU (different streams, or different host threads)
+ * race and corrupt each other's results.  The call waits for its work and
+ * returns device-side errors like the timed entry points. */
+#define GQF_NOALLOC_MAX_KEYS (1u << 20)
+#define GQF_NOALLOC_MAX_Q 22
+#define GQF_NOALLOC_SCRATCH_BYTES (12u << 20)
+int gqf_sqf_bulk_build_noalloc(const gqf_sqf *qf, int n, const uint32_t *d_keys,
+                               int no_duplicates, void *stream);
 
 /* ---------------- rank-and-select quotient filter ----------------------- */
 /* initCQFGPU, RSQF.cu:32-40 (zeroed blocks + one guard block) */
