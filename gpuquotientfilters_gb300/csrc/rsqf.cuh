@@ -1,0 +1,363 @@
+// Rank-and-select quotient filter (RSQF) device code.
+//
+// Storage is the reference's own packed block layout (RSQF.cuh:24-30):
+// 57 bytes per block = u8 offset, u64 occupieds, u64 runEnds, u64
+// remainders[5] (5-bit fields, slot s at bit 5s, little-endian), so a table
+// written here is byte-identical to the reference's.  One zeroed guard block
+// follows the calcNumBlocksGPU() logical blocks: the reference's bounds
+// checks (`blockNum > numBlocks`, RSQF.cu:359,578) let it touch that index.
+//
+// Lookups restate lookupGPU (RSQF.cu:320-399): rank of the quotient's
+// occupied bit, select of the matching run end (continuing into following
+// blocks), then a backward walk through the run.  Rank is __popcll and
+// select a popcount-guided binary split instead of the reference's
+// broadword byte-table select (kSelectInByte, RSQF.cu:214-318).
+//
+// Inserts restate the reference's sequential insert (insertIntoRegions,
+// RSQF.cu:645-875, = insert, RSQF.cpp:367-520) exactly, including its
+// handling of the `offset` byte and of findFirstUnusedSlot's rank == 0
+// case, because the reference's layout after an incremental batch depends
+// on that order-sensitive code (it is not a pure function of the
+// fingerprint multiset).  Parallelism comes from running independent groups
+// of blocks at once; see rsqf_api.cu.
+#pragma once
+
+#include "qf_device.cuh"
+
+namespace gqf {
+
+constexpr uint32_t RSQF_BB = 57;   // bytes per packed block
+constexpr uint32_t RSQF_R = 5;     // remainder bits (RSQF.cuh:21)
+constexpr uint32_t RSQF_SPB = 64;  // slots per block (RSQF.cuh:22)
+constexpr uint32_t RSQF_NONE = 0xFFFFFFFFu;
+
+__host__ __device__ inline size_t rsqf_table_bytes(uint32_t nblocks)
+{
+    // logical blocks + guard block + 16 bytes so 8-byte reads near the end
+    // stay inside the allocation
+    return (size_t)(nblocks + 1) * RSQF_BB + 16;
+}
+
+__device__ __forceinline__ uint64_t ld_u64_unaligned(const uint8_t *p)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uint64_t *w = reinterpret_cast<const uint64_t *>(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8;
+    uint64_t lo = w[0];
+    if (!sh) return lo;
+    uint64_t hi = w[1];
+    return (lo >> sh) | (hi << (64 - sh));
+}
+__device__ __forceinline__ void st_u64_bytes(uint8_t *p, uint64_t v)
+{
+#pragma unroll
+    for (int k = 0; k < 8; k++) p[k] = (uint8_t)(v >> (8 * k));
+}
+
+__device__ __forceinline__ uint64_t lowmask64(uint32_t n) { return n >= 64 ? ~0ull : ((1ull << n) - 1ull); }
+
+// position of the k-th set bit (k >= 1) of x; RSQF_NONE if x has fewer than
+// k ones; 0 when k == 0 (the reference's selectBitGPU contract, RSQF.cu:260)
+__device__ __forceinline__ uint32_t select64(uint64_t x, uint32_t k)
+{
+    if (k == 0) return 0;
+    if (k > (uint32_t)__popcll(x)) return RSQF_NONE;
+    uint32_t base = 0;
+    uint32_t c = __popc((uint32_t)x);
+    if (k > c) {
+        k -= c;
+        x >>= 32;
+        base = 32;
+    }
+    uint32_t v = (uint32_t)x;
+    c = __popc(v & 0xFFFFu);
+    if (k > c) {
+        k -= c;
+        v >>= 16;
+        base += 16;
+    }
+    c = __popc(v & 0xFFu);
+    if (k > c) {
+        k -= c;
+        v >>= 8;
+        base += 8;
+    }
+    for (uint32_t i = 1; i < k; i++) v &= v - 1;
+    return base + (uint32_t)(__ffs(v) - 1);
+}
+__device__ __forceinline__ uint32_t rank64(uint64_t x, uint32_t i)  // ones in [0, i]
+{
+    return (uint32_t)__popcll(x & lowmask64(i + 1));
+}
+
+// Read-only view of a packed table.
+struct RsqfView {
+    const uint8_t *t;
+    uint32_t nblocks;  // logical blocks (the guard block is index nblocks)
+    __device__ __forceinline__ const uint8_t *blk(uint32_t b) const { return t + (size_t)b * RSQF_BB; }
+    __device__ __forceinline__ uint32_t off(uint32_t b) const { return blk(b)[0]; }
+    __device__ __forceinline__ uint64_t occ(uint32_t b) const { return ld_u64_unaligned(blk(b) + 1); }
+    __device__ __forceinline__ uint64_t re(uint32_t b) const { return ld_u64_unaligned(blk(b) + 9); }
+    __device__ __forceinline__ uint32_t rem(uint32_t b, uint32_t s) const
+    {
+        uint32_t bit = s * RSQF_R;
+        return (uint32_t)(ld_u64_unaligned(blk(b) + 17 + (bit >> 3)) >> (bit & 7)) & 31u;
+    }
+};
+
+// lookupGPU (RSQF.cu:320-399) for fingerprint fp: slot or -1.
+__device__ inline int32_t rsqf_lookup(const RsqfView &v, uint32_t q, uint32_t fp)
+{
+    const uint32_t fq = (fp >> RSQF_R) & ((1u << q) - 1u);
+    const uint32_t fr = fp & 31u;
+    uint32_t b = fq / RSQF_SPB, sl = fq % RSQF_SPB;
+    uint64_t occ = v.occ(b);
+    if (!((occ >> sl) & 1ull)) return -1;
+    uint32_t off = v.off(b);
+    uint32_t rank = rank64(occ, sl);
+    uint64_t re = v.re(b);
+    uint32_t end = select64(re & ~lowmask64(off), rank);
+    while (end == RSQF_NONE) {
+        rank -= (uint32_t)__popcll(re & ~lowmask64(off));
+        off = (int)off - (int)RSQF_SPB > 0 ? off - RSQF_SPB : 0u;
+        b++;
+        if (b > v.nblocks) return -1;
+        re = v.re(b);
+        end = select64(re & ~lowmask64(off), rank);
+    }
+    uint32_t cur = end;
+    uint32_t rem = v.rem(b, cur);
+    for (;;) {
+        if (rem == fr) return (int32_t)(b * RSQF_SPB + cur);
+        if (rem < fr) return -1;
+        if (cur > 0) {
+            cur--;
+        } else {
+            cur = RSQF_SPB - 1;
+            if (b == 0) return -1;
+            b--;
+        }
+        rem = v.rem(b, cur);
+        if (((v.re(b) >> cur) & 1ull) || b * RSQF_SPB + cur < fq) return -1;
+    }
+}
+
+constexpr int RSQF_LOOKUP_THREADS = 256;
+
+__global__ void __launch_bounds__(RSQF_LOOKUP_THREADS) k_rsqf_lookup_unsorted(const uint32_t *__restrict__ keys,
+                                                                             uint32_t n, RsqfView v, uint32_t q,
+                                                                             int32_t *__restrict__ out)
+{
+    const uint32_t mask = (1u << (q + RSQF_R)) - 1u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = rsqf_lookup(v, q, aphash32(__ldg(keys + i)) & mask);
+}
+
+// launchLookups: queries grouped by quotient range (bucketed (fp, index)
+// pairs), results written to their input positions.
+__global__ void __launch_bounds__(RSQF_LOOKUP_THREADS) k_rsqf_lookup_bucketed(
+    const uint32_t *__restrict__ items, const uint32_t *__restrict__ idx, const uint32_t *__restrict__ base,
+    const uint32_t *__restrict__ cnt, RsqfView v, uint32_t q, int32_t *__restrict__ out)
+{
+    const uint32_t b = blockIdx.x;
+    const uint32_t n = cnt[b];
+    const size_t s0 = base[b];
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[idx[s0 + i]] = rsqf_lookup(v, q, items[s0 + i]);
+}
+
+// ----------------------------------------------------------------------------
+// Insert emulation.  A group is a run of blocks [glo, ghi); its thread inserts
+// the group's batch items (ascending fingerprints) with the reference's
+// sequential algorithm.  Blocks right of the group are read from the
+// pre-batch copy t0 (in the sequential order no earlier item has touched
+// them unless it crossed); any write outside [glo, ghi) marks the group as
+// crossed and stops it (the host merges it with its successor and reruns).
+// ----------------------------------------------------------------------------
+struct RsqfGroupTable {
+    uint8_t *t;         // live table
+    const uint8_t *t0;  // table before the batch
+    uint32_t nblocks;
+    uint32_t glo, ghi;  // this group's blocks
+    bool crossed;
+    __device__ __forceinline__ const uint8_t *rd(uint32_t b) const
+    {
+        return (b >= glo && b < ghi) ? t + (size_t)b * RSQF_BB : t0 + (size_t)b * RSQF_BB;
+    }
+    __device__ __forceinline__ uint8_t *wr(uint32_t b)
+    {
+        if (b < glo || b >= ghi) {
+            crossed = true;
+            return nullptr;
+        }
+        return t + (size_t)b * RSQF_BB;
+    }
+    __device__ __forceinline__ uint32_t off(uint32_t b) const { return rd(b)[0]; }
+    __device__ __forceinline__ uint64_t occ(uint32_t b) const { return ld_u64_unaligned(rd(b) + 1); }
+    __device__ __forceinline__ uint64_t re(uint32_t b) const { return ld_u64_unaligned(rd(b) + 9); }
+    __device__ __forceinline__ uint32_t rem(uint32_t b, uint32_t s) const
+    {
+        uint32_t bit = s * RSQF_R;
+        return (uint32_t)(ld_u64_unaligned(rd(b) + 17 + (bit >> 3)) >> (bit & 7)) & 31u;
+    }
+    __device__ __forceinline__ void set_off(uint32_t b, uint32_t v)
+    {
+        uint8_t *p = wr(b);
+        if (p) p[0] = (uint8_t)v;
+    }
+    __device__ __forceinline__ void set_occ(uint32_t b, uint64_t v)
+    {
+        uint8_t *p = wr(b);
+        if (p) st_u64_bytes(p + 1, v);
+    }
+    __device__ __forceinline__ void set_re(uint32_t b, uint64_t v)
+    {
+        uint8_t *p = wr(b);
+        if (p) st_u64_bytes(p + 9, v);
+    }
+    __device__ __forceinline__ void set_rem(uint32_t b, uint32_t s, uint32_t val)
+    {
+        uint8_t *p = wr(b);
+        if (!p) return;
+        uint32_t bit = s * RSQF_R;
+        uint8_t *q = p + 17 + (bit >> 3);
+        uint32_t sh = bit & 7;
+        uint32_t w = (uint32_t)q[0] | ((uint32_t)q[1] << 8);  // a field spans at most 2 bytes
+        w = (w & ~(31u << sh)) | ((val & 31u) << sh);
+        q[0] = (uint8_t)w;
+        if (sh > 3) q[1] = (uint8_t)(w >> 8);
+    }
+};
+
+// findFirstUnusedSlot (RSQF.cpp:341-365; RSQF.cu:565-590), rank == 0 case
+// included as written there.
+__device__ inline uint32_t rsqf_first_unused(RsqfGroupTable &f, int &bn, uint32_t start)
+{
+    uint32_t cur = start;
+    uint64_t occ = f.occ((uint32_t)bn), re = f.re((uint32_t)bn);
+    uint32_t off = f.off((uint32_t)bn);
+    uint32_t rank = rank64(occ, start);
+    uint32_t sel = select64(re & ~lowmask64(off), rank);
+    if (rank == 0) sel = off;
+    // every pass advances cur; the cap only bounds a corrupted table
+    for (uint32_t guard = 0; cur <= sel; guard++) {
+        if (guard > 64u * (f.nblocks + 2)) return RSQF_NONE;
+        if (sel == RSQF_NONE || sel == RSQF_SPB - 1) {
+            bn++;
+            if ((uint32_t)bn > f.nblocks) return RSQF_NONE;
+            occ = f.occ((uint32_t)bn);
+            re = f.re((uint32_t)bn);
+            off = f.off((uint32_t)bn);
+            sel = off - 1u;
+        }
+        cur = sel + 1;
+        rank = rank64(occ, cur);
+        sel = select64(re & ~lowmask64(off), rank);
+    }
+    return cur;
+}
+
+// insert (RSQF.cpp:367-520 = RSQF.cu:645-875 per item): slot or -1.  On a
+// crossing f.crossed is set and the return value is meaningless.
+__device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp)
+{
+    const uint32_t fq = (fp >> RSQF_R) & ((1u << q) - 1u);
+    const uint32_t fr = fp & 31u;
+    const int home = (int)(fq / RSQF_SPB);
+    int bn = home;
+    const uint32_t hs = fq % RSQF_SPB;
+    const uint64_t occ = f.occ((uint32_t)bn);
+    uint32_t off = f.off((uint32_t)bn);
+    uint32_t rank = rank64(occ, hs);
+    const uint64_t re = f.re((uint32_t)bn);
+    uint32_t end = select64(re & ~lowmask64(off), rank);
+    if (rank == 0) end = off == 0 ? 0u : off - 1u;
+    while (end == RSQF_NONE) {
+        rank -= (uint32_t)__popcll(f.re((uint32_t)bn) & ~lowmask64(off));
+        off = (int)off - (int)RSQF_SPB > 0 ? off - RSQF_SPB : 0u;
+        bn++;
+        if ((uint32_t)bn > f.nblocks) return -1;  // past the guard block (the reference reads beyond)
+        end = select64(f.re((uint32_t)bn) & ~lowmask64(off), rank);
+    }
+    if (((uint32_t)bn * RSQF_SPB + end < (uint32_t)home * RSQF_SPB + hs) | (off + rank == 0)) {
+        f.set_re((uint32_t)home, re | (1ull << hs));
+        f.set_rem((uint32_t)home, hs, fr);
+        f.set_occ((uint32_t)home, occ | (1ull << hs));
+        return (int32_t)((uint32_t)home * RSQF_SPB + hs);
+    }
+    end++;
+    if (end == RSQF_SPB) {
+        end = 0;
+        bn++;
+        if ((uint32_t)bn > f.nblocks) return -1;
+    }
+    const int re_block = bn;
+    uint32_t unused = rsqf_first_unused(f, bn, end);
+    if (unused == RSQF_NONE) return -1;
+    if (bn > home)
+        for (int i = 0; i < bn - home; i++) f.set_off((uint32_t)(bn - i), f.off((uint32_t)(bn - i)) + 1u);
+    while ((uint32_t)bn * RSQF_SPB + unused > (uint32_t)re_block * RSQF_SPB + end) {
+        if (f.crossed) return -1;
+        if (unused == 0) {
+            const int nb = bn - 1;
+            const uint32_t ns = RSQF_SPB - 1;
+            f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)nb, ns));
+            uint64_t r2 = f.re((uint32_t)bn);
+            f.set_re((uint32_t)bn, ((f.re((uint32_t)nb) >> ns) & 1ull) ? (r2 | 1ull) : (r2 & ~1ull));
+            unused = RSQF_SPB - 1;
+            bn--;
+        } else {
+            f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)bn, unused - 1));
+            uint64_t r2 = f.re((uint32_t)bn);
+            f.set_re((uint32_t)bn, ((r2 >> (unused - 1)) & 1ull) ? (r2 | (1ull << unused)) : (r2 & ~(1ull << unused)));
+            unused--;
+        }
+    }
+    if (!((f.occ((uint32_t)home) >> hs) & 1ull)) {
+        f.set_rem((uint32_t)bn, unused, fr);
+        f.set_re((uint32_t)bn, f.re((uint32_t)bn) | (1ull << unused));
+        f.set_occ((uint32_t)home, f.occ((uint32_t)home) | (1ull << hs));
+        return (int32_t)((uint32_t)bn * RSQF_SPB + unused);
+    }
+    uint32_t ns = unused - 1;
+    int nb = bn;
+    if (unused == 0) {
+        ns = RSQF_SPB - 1;
+        nb = bn - 1;
+        if (nb < 0) return -1;
+    }
+    f.set_re((uint32_t)bn, f.re((uint32_t)bn) | (1ull << unused));
+    f.set_re((uint32_t)nb, f.re((uint32_t)nb) & ~(1ull << ns));
+    uint32_t nrem = f.rem((uint32_t)nb, ns);
+    for (;;) {
+        if (f.crossed) return -1;
+        if (nrem <= fr) {
+            f.set_rem((uint32_t)bn, unused, fr);
+            return (int32_t)((uint32_t)bn * RSQF_SPB + unused);
+        }
+        f.set_rem((uint32_t)bn, unused, nrem);
+        if (unused > 0) {
+            unused--;
+            if (unused == 0) {
+                if (bn == 0) {
+                    f.set_rem((uint32_t)bn, unused, fr);
+                    return (int32_t)((uint32_t)bn * RSQF_SPB + unused);
+                }
+                ns = RSQF_SPB - 1;
+                nb--;
+            } else {
+                ns = unused - 1;
+            }
+        } else {
+            unused = RSQF_SPB - 1;
+            bn--;
+            if (bn < 0) return -1;
+            ns = unused - 1;
+        }
+        nrem = f.rem((uint32_t)nb, ns);
+        if (((f.re((uint32_t)nb) >> ns) & 1ull) || (uint32_t)nb * RSQF_SPB + ns < fq) break;
+    }
+    f.set_rem((uint32_t)bn, unused, fr);
+    return (int32_t)((uint32_t)bn * RSQF_SPB + unused);
+}
+
+}  // namespace gqf

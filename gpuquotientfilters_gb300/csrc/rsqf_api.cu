@@ -1,11 +1,378 @@
-// C ABI of the rank-and-select quotient filter (placeholder entry points).
+// C ABI of the rank-and-select quotient filter: host orchestration.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "host_common.cuh"
+#include "rsqf.cuh"
+#include "sqf_build.cuh"
+
+namespace gqf {
+
+static bool rsqf_q_ok(unsigned q) { return q >= 7 && q + RSQF_R <= 31; }
+
+static uint32_t ceil_log2u(uint64_t x)
+{
+    uint32_t l = 0;
+    while ((1ull << l) < x) l++;
+    return l;
+}
+
+// Bucket geometry for RSQF batches (fingerprint = quotient << 5 | remainder,
+// the SQF r = 5 layout): ~12k items per bucket, at most 4096 buckets.
+static BucketGeom rsqf_geom(uint32_t q, uint64_t n)
+{
+    BucketGeom g;
+    uint32_t tb_lo = std::max<uint32_t>(7, q > 12 ? q - 12 : 0);
+    uint32_t tb_hi = std::min<uint32_t>(q, 15);
+    uint32_t tb = ceil_log2u((12000ull << q) / (n ? n : 1));
+    tb = std::min(std::max(tb, tb_lo), tb_hi);
+    g.q = q;
+    g.r = RSQF_R;
+    g.tb = tb;
+    g.nb = 1u << (q - tb);
+    g.shift = RSQF_R + tb;
+    g.fp_mask = (1u << (q + RSQF_R)) - 1u;
+    return g;
+}
+
+template <typename K>
+static cudaError_t set_smem(K kernel, size_t bytes)
+{
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+__global__ void __launch_bounds__(1024) k_rsqf_scan_bases(const uint32_t *cnt, uint32_t nb, uint32_t *base)
+{
+    __shared__ uint32_t s[4097];
+    __shared__ uint32_t sw[33];
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) s[i] = cnt[i];
+    __syncthreads();
+    uint32_t tot = block_exclusive_scan_u32<1024>(s, nb, sw);
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) base[i] = s[i];
+    if (threadIdx.x == 0) base[nb] = tot;
+}
+
+// Sorts each bucket of fingerprints in place (exact bucket bases, so the
+// whole array ends up sorted): counting sort by local quotient in shared
+// memory, then the (small) groups of equal quotient by value.
+constexpr int SORT_THREADS = 512;
+__host__ __device__ inline size_t sort_smem_bytes(uint32_t tb, uint32_t cap)
+{
+    size_t S = (size_t)1 << tb;
+    return 4 * (S / 2 + S / 32 + 8) + 4 * (size_t)cap;
+}
+__global__ void __launch_bounds__(SORT_THREADS) k_bucket_sort(uint32_t *items, const uint32_t *base,
+                                                             const uint32_t *cnt, uint32_t tb, uint32_t cap,
+                                                             uint32_t *err)
+{
+    extern __shared__ __align__(16) uint32_t smem_sort[];
+    const uint32_t S = 1u << tb;
+    uint32_t *s_cnt = smem_sort;
+    uint32_t *s_it = smem_sort + (S / 2 + S / 32 + 8);
+    __shared__ uint32_t s_warp[33];
+    const uint32_t b = blockIdx.x, n = cnt[b];
+    const size_t b0 = base[b];
+    if (n <= 1) return;
+    if (n > cap) {
+        if (threadIdx.x == 0) atomicOr(err, DEV_ERR_BUCKET_CAP);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < S / 2 + S / 32 + 8; i += SORT_THREADS) s_cnt[i] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += SORT_THREADS) cnt16_fetch_inc(s_cnt, (items[b0 + i] >> RSQF_R) & (S - 1));
+    __syncthreads();
+    // exclusive scan of the packed u16 counters, S/2 words in skewed order
+    {
+        const uint32_t per = (S + SORT_THREADS - 1) / SORT_THREADS;  // quotients per thread (even or 1)
+        const uint32_t q0 = min(S, threadIdx.x * per), q1 = min(S, q0 + per);
+        uint32_t sum = 0;
+        for (uint32_t x = q0; x < q1; x++) sum += cnt16_get(s_cnt, x);
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) s_warp[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t v = lane < SORT_THREADS / 32 ? s_warp[lane] : 0, iv = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, iv, o);
+                if (lane >= o) iv += t;
+            }
+            if (lane < SORT_THREADS / 32) s_warp[lane] = iv - v;
+        }
+        __syncthreads();
+        uint32_t run = s_warp[wid] + incl - sum;
+        __syncthreads();
+        for (uint32_t x = q0; x < q1; x++) {
+            uint32_t c = cnt16_get(s_cnt, x);
+            uint32_t w = skew16(x >> 1), sh = (x & 1) * 16;
+            s_cnt[w] = (s_cnt[w] & ~(0xFFFFu << sh)) | (run << sh);
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += SORT_THREADS) {
+        uint32_t v = items[b0 + i];
+        s_it[cnt16_fetch_inc(s_cnt, (v >> RSQF_R) & (S - 1))] = v;
+    }
+    __syncthreads();
+    for (uint32_t x = threadIdx.x; x < S; x += SORT_THREADS) {
+        uint32_t g0 = x ? cnt16_get(s_cnt, x - 1) : 0u, g1 = cnt16_get(s_cnt, x);
+        if (g1 - g0 > 1) small_sort(s_it + g0, g1 - g0);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += SORT_THREADS) items[b0 + i] = s_it[i];
+}
+
+// blk_start[b] = first sorted index whose home block is >= b (b <= nbl).
+__global__ void k_block_starts(const uint32_t *__restrict__ fps, uint32_t n, uint32_t nbl,
+                               uint32_t *__restrict__ blk_start)
+{
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= nbl; b += gridDim.x * blockDim.x) {
+        uint64_t key = (uint64_t)b * RSQF_SPB << RSQF_R;
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if ((uint64_t)fps[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        blk_start[b] = lo;
+    }
+}
+
+// One emulation round: every active group (start[b] && active[b]) restores
+// its blocks from t0 and inserts its items in ascending order.
+__global__ void k_rsqf_round(uint8_t *t, const uint8_t *t0, uint32_t nblocks, uint32_t q, const uint32_t *fps,
+                             const uint32_t *blk_start, const uint8_t *start, uint8_t *active, uint8_t *crossed,
+                             uint32_t *n_crossed, int32_t *ret)
+{
+    const uint32_t total = nblocks + 1;  // logical blocks + guard block
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
+        if (!start[b] || !active[b]) continue;
+        uint32_t e = b + 1;
+        while (e < total && !start[e]) e++;
+        // restore this group's blocks
+        for (size_t i = (size_t)b * RSQF_BB; i < (size_t)e * RSQF_BB; i++) t[i] = t0[i];
+        RsqfGroupTable f{t, t0, nblocks, b, e, false};
+        const uint32_t nbl_items = (nblocks - 1);  // blocks that can be homes
+        const uint32_t i0 = blk_start[min(b, nbl_items)], i1 = blk_start[min(e, nbl_items)];
+        bool cross = false;
+        for (uint32_t i = i0; i < i1; i++) {
+            int32_t s = rsqf_insert(f, q, fps[i]);
+            if (f.crossed) {
+                cross = true;
+                break;
+            }
+            ret[i] = s;
+        }
+        crossed[b] = cross ? 1 : 0;
+        active[b] = 0;
+        if (cross) atomicAdd(n_crossed, 1u);
+    }
+}
+
+// Merge every crossed group with its successor (chains collapse in one
+// pass) and mark the merged groups active for the next round.
+__global__ void k_rsqf_merge(uint32_t nblocks, uint8_t *start, uint8_t *active, uint8_t *crossed)
+{
+    const uint32_t total = nblocks + 1;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
+        if (!start[b] || !crossed[b]) continue;
+        uint32_t e = b + 1;
+        while (e < total && !start[e]) e++;
+        if (e < total) start[e] = 0;  // successor joins this group
+        active[b] = 1;
+        crossed[b] = 0;
+    }
+}
+
+}  // namespace gqf
+
+using namespace gqf;
 
 extern "C" {
+
 size_t gqf_rsqf_num_blocks(unsigned int q) { return (((size_t)1u << q) + 63) / 64 + 1; }
-int gqf_rsqf_init(gqf_rsqf *cqf, unsigned int q) { (void)cqf; (void)q; return GQF_ERR_ARG; }
-int gqf_rsqf_free(gqf_rsqf *cqf) { (void)cqf; return GQF_ERR_ARG; }
-int gqf_rsqf_insert(const gqf_rsqf *, int, const uint32_t *, int32_t *, void *, float *) { return GQF_ERR_ARG; }
-int gqf_rsqf_lookup_sorted(const gqf_rsqf *, int, const uint32_t *, int32_t *, void *, float *) { return GQF_ERR_ARG; }
-int gqf_rsqf_lookup_unsorted(const gqf_rsqf *, int, const uint32_t *, int32_t *, void *, float *) { return GQF_ERR_ARG; }
+
+int gqf_rsqf_init(gqf_rsqf *cqf, unsigned int q)
+{
+    if (!cqf || !rsqf_q_ok(q)) return GQF_ERR_ARG;
+    cqf->qbits = q;
+    cqf->numBlocks = (unsigned)gqf_rsqf_num_blocks(q);
+    size_t bytes = rsqf_table_bytes(cqf->numBlocks);
+    void *p = nullptr;
+    GQF_CK(cudaMalloc(&p, bytes));
+    GQF_CK(cudaMemset(p, 0, bytes));
+    cqf->blocks = p;
+    return GQF_OK;
 }
+
+int gqf_rsqf_free(gqf_rsqf *cqf)
+{
+    if (!cqf) return GQF_ERR_ARG;
+    if (cqf->blocks) GQF_CK(cudaFree(cqf->blocks));
+    cqf->blocks = nullptr;
+    return GQF_OK;
+}
+
+static bool rsqf_ok(const gqf_rsqf *c)
+{
+    return c && c->blocks && rsqf_q_ok(c->qbits) && c->numBlocks == gqf_rsqf_num_blocks(c->qbits);
+}
+
+int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_out, void *stream,
+                             float *ms)
+{
+    if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Arena &ar = arena(current_device());
+    std::lock_guard<std::mutex> lk(ar.mu);
+    int st = call_begin(ar, s, ms != nullptr);
+    if (st) return st;
+    if (n > 0) {
+        RsqfView v{static_cast<const uint8_t *>(cqf->blocks), cqf->numBlocks};
+        const DeviceInfo &di = device_info(current_device());
+        uint32_t grid = std::min<uint32_t>((n + RSQF_LOOKUP_THREADS - 1) / RSQF_LOOKUP_THREADS, di.sms * 32);
+        k_rsqf_lookup_unsorted<<<grid, RSQF_LOOKUP_THREADS, 0, s>>>(d_keys, (uint32_t)n, v, cqf->qbits, d_out);
+        count_launches(1);
+    }
+    return call_end(ar, s, ms);
+}
+
+// Hash + exact bucketing of a batch into (items, optional idx, base, cnt).
+static int rsqf_bucket(const uint32_t *keys, uint32_t n, const BucketGeom &g, uint32_t *items, uint32_t *idx,
+                       uint32_t *cnt, uint32_t *base, uint32_t *err, cudaStream_t s)
+{
+    GQF_CK(cudaMemsetAsync(cnt, 0, g.nb * 4, s));
+    const uint32_t hchunk = SCATTER_THREADS * SCATTER_IPT;
+    GQF_CK(set_smem(k_bucket_hist<SCATTER_THREADS, SCATTER_IPT>, g.nb * 4));
+    k_bucket_hist<SCATTER_THREADS, SCATTER_IPT><<<(n + hchunk - 1) / hchunk, SCATTER_THREADS, g.nb * 4, s>>>(
+        keys, n, g, cnt);
+    k_rsqf_scan_bases<<<1, 1024, 0, s>>>(cnt, g.nb, base);
+    GQF_CK(cudaMemsetAsync(cnt, 0, g.nb * 4, s));
+    if (idx) {
+        auto kfn = k_hash_bucket<PAIR_THREADS, PAIR_IPT, true>;
+        size_t sm = (size_t)2 * PAIR_THREADS * PAIR_IPT * 4 + (size_t)g.nb * 8;
+        GQF_CK(set_smem(kfn, sm));
+        const uint32_t chunk = PAIR_THREADS * PAIR_IPT;
+        kfn<<<(n + chunk - 1) / chunk, PAIR_THREADS, sm, s>>>(keys, n, g, base, 0xFFFFFFFFu, cnt, items, idx, err);
+    } else {
+        auto kfn = k_hash_bucket<SCATTER_THREADS, SCATTER_IPT, false>;
+        size_t sm = (size_t)SCATTER_THREADS * SCATTER_IPT * 4 + (size_t)g.nb * 8;
+        GQF_CK(set_smem(kfn, sm));
+        kfn<<<(n + hchunk - 1) / hchunk, SCATTER_THREADS, sm, s>>>(keys, n, g, base, 0xFFFFFFFFu, cnt, items,
+                                                                   nullptr, err);
+    }
+    count_launches(3);
+    GQF_CK(cudaGetLastError());
+    return GQF_OK;
+}
+
+int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_out, void *stream,
+                           float *ms)
+{
+    if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const BucketGeom g = rsqf_geom(cqf->qbits, (uint64_t)n);
+    Arena &ar = arena(current_device());
+    std::lock_guard<std::mutex> lk(ar.mu);
+    Sizer z;
+    z.take<uint32_t>(g.nb);
+    z.take<uint32_t>(g.nb + 1);
+    z.take<uint32_t>(std::max(n, 1));
+    z.take<uint32_t>(std::max(n, 1));
+    void *basep = arena_reserve(ar, z.off);
+    if (!basep) return GQF_ERR_NOMEM;
+    Carver c(basep);
+    uint32_t *cnt = c.take<uint32_t>(g.nb), *base = c.take<uint32_t>(g.nb + 1);
+    uint32_t *items = c.take<uint32_t>(std::max(n, 1)), *idx = c.take<uint32_t>(std::max(n, 1));
+    int st = call_begin(ar, s, ms != nullptr);
+    if (st) return st;
+    if (n > 0) {
+        st = rsqf_bucket(d_keys, (uint32_t)n, g, items, idx, cnt, base, ar.err, s);
+        if (st) return st;
+        RsqfView v{static_cast<const uint8_t *>(cqf->blocks), cqf->numBlocks};
+        k_rsqf_lookup_bucketed<<<g.nb, RSQF_LOOKUP_THREADS, 0, s>>>(items, idx, base, cnt, v, cqf->qbits, d_out);
+        count_launches(1);
+    }
+    return call_end(ar, s, ms);
+}
+
+// insertGPU (RSQF.cu:882-988).  The batch is sorted, then the reference's
+// sequential insert is replayed group by group (see k_rsqf_round); groups
+// whose inserts spill past their last block are merged with their successor
+// and replayed from the pre-batch table until no group spills.
+int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_ret, void *stream, float *ms)
+{
+    if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_ret))) return GQF_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint32_t q = cqf->qbits, nbl = cqf->numBlocks;
+    const BucketGeom g = rsqf_geom(q, (uint64_t)n);
+    const size_t tbytes = rsqf_table_bytes(nbl);
+    Arena &ar = arena(current_device());
+    std::lock_guard<std::mutex> lk(ar.mu);
+    Sizer z;
+    z.take<uint32_t>(g.nb);
+    z.take<uint32_t>(g.nb + 1);
+    z.take<uint32_t>(std::max(n, 1));
+    z.take<uint32_t>(nbl + 2);
+    z.take<uint8_t>(tbytes);
+    z.take<uint8_t>(nbl + 1);
+    z.take<uint8_t>(nbl + 1);
+    z.take<uint8_t>(nbl + 1);
+    z.take<uint32_t>(1);
+    void *basep = arena_reserve(ar, z.off);
+    if (!basep) return GQF_ERR_NOMEM;
+    Carver c(basep);
+    uint32_t *cnt = c.take<uint32_t>(g.nb), *base = c.take<uint32_t>(g.nb + 1);
+    uint32_t *items = c.take<uint32_t>(std::max(n, 1)), *blk_start = c.take<uint32_t>(nbl + 2);
+    uint8_t *t0 = c.take<uint8_t>(tbytes), *start = c.take<uint8_t>(nbl + 1), *active = c.take<uint8_t>(nbl + 1),
+            *crossed = c.take<uint8_t>(nbl + 1);
+    uint32_t *ncross = c.take<uint32_t>(1);
+    int st = call_begin(ar, s, true);
+    if (st) return st;
+    if (n > 0) {
+        st = rsqf_bucket(d_keys, (uint32_t)n, g, items, nullptr, cnt, base, ar.err, s);
+        if (st) return st;
+        const uint32_t S = 1u << g.tb;
+        const DeviceInfo &di = device_info(current_device());
+        // per-bucket sort: capacity from the largest bucket the smem allows
+        size_t maxsm = (size_t)(di.smem_optin > 0 ? di.smem_optin : 99 * 1024) - 2048;
+        size_t fixed = sort_smem_bytes(g.tb, 0);
+        uint32_t cap = maxsm > fixed ? (uint32_t)std::min<size_t>((maxsm - fixed) / 4, 65535) : 0;
+        size_t sm = sort_smem_bytes(g.tb, cap);
+        GQF_CK(set_smem(k_bucket_sort, sm));
+        k_bucket_sort<<<g.nb, SORT_THREADS, sm, s>>>(items, base, cnt, g.tb, cap, ar.err);
+        (void)S;
+        k_block_starts<<<(nbl + 2 + 255) / 256, 256, 0, s>>>(items, (uint32_t)n, nbl - 1, blk_start);
+        GQF_CK(cudaMemcpyAsync(t0, cqf->blocks, tbytes, cudaMemcpyDeviceToDevice, s));
+        // initial groups of 4 blocks
+        std::vector<uint8_t> h_start(nbl + 1, 0);
+        for (uint32_t b = 0; b <= nbl; b += 4) h_start[b] = 1;
+        GQF_CK(cudaMemcpyAsync(start, h_start.data(), nbl + 1, cudaMemcpyHostToDevice, s));
+        GQF_CK(cudaMemcpyAsync(active, h_start.data(), nbl + 1, cudaMemcpyHostToDevice, s));
+        GQF_CK(cudaMemsetAsync(crossed, 0, nbl + 1, s));
+        count_launches(2);
+        const uint32_t grid = std::min<uint32_t>((nbl + 1 + 127) / 128, di.sms * 16);
+        for (int round = 0;; round++) {
+            GQF_CK(cudaMemsetAsync(ncross, 0, 4, s));
+            k_rsqf_round<<<grid, 128, 0, s>>>(static_cast<uint8_t *>(cqf->blocks), t0, nbl, q, items, blk_start,
+                                             start, active, crossed, ncross, d_ret);
+            count_launches(1);
+            uint32_t h_n = 0;
+            GQF_CK(cudaMemcpyAsync(&h_n, ncross, 4, cudaMemcpyDeviceToHost, s));
+            GQF_CK(cudaStreamSynchronize(s));
+            if (h_n == 0) break;
+            if (round > 100000) return GQF_ERR_TIMEOUT;
+            k_rsqf_merge<<<grid, 128, 0, s>>>(nbl, start, active, crossed);
+            count_launches(1);
+        }
+    }
+    return call_end(ar, s, ms ? ms : nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+"""RSQF parity on the GPU: packed blocks byte-identical to the oracle (the
+reference CPU_version restated, pinned by its golden digests) after every
+insert batch, return slots identical, lookups identical."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+class RSQF:
+    def __init__(self, G, torch, q):
+        self.G, self.torch, self.q = G, torch, q
+        self.cqf = G.initCQFGPU(q)
+
+    def __del__(self):
+        try:
+            self.G.freeCQFGPU(self.cqf)
+        except Exception:
+            pass
+
+    def insert(self, keys):
+        ret = self.torch.empty(max(keys.size, 1), dtype=self.torch.int32, device="cuda")
+        self.G.insertGPU(self.cqf, keys.size, to_dev(self.torch, keys), ret)
+        return ret.cpu().numpy()[: keys.size]
+
+    def lookup(self, keys, sorted_=True):
+        out = self.torch.empty(keys.size, dtype=self.torch.int32, device="cuda")
+        fn = self.G.launchLookups if sorted_ else self.G.launchUnsortedLookupsRSQF
+        fn(self.cqf, keys.size, to_dev(self.torch, keys), out)
+        return out.cpu().numpy()
+
+    def blocks(self):
+        return self.G.rsqf_blocks_bytes(self.cqf)
+
+
+def assert_same_blocks(g, o):
+    if not np.array_equal(g, o):
+        d = np.nonzero(g != o)[0]
+        raise AssertionError("%d bytes differ, first at %d (block %d byte %d)" % (d.size, d[0], d[0] // 57, d[0] % 57))
+
+
+@pytest.mark.parametrize("case", GOLDEN["rsqf_cpu_version"], ids=lambda c: "q%d_n%d" % (c["q"], c["n"]))
+def test_rsqf_golden(gqf, cuda, case):
+    q, n, batch, seed = case["q"], case["n"], case["batch"], case["seed"]
+    f = RSQF(gqf, cuda, q)
+    keys = O.mt_keys(seed, n)
+    ret = f.insert(keys)
+    assert sha(f.blocks()) == case["build_blocks_sha256"]
+    assert sha(ret) == case["build_rets_sha256"]
+    bret = f.insert(O.mt_keys(seed, batch, skip=n))
+    assert sha(f.blocks()) == case["batch_blocks_sha256"]
+    assert sha(bret) == case["batch_rets_sha256"]
+    look = np.concatenate([keys[: case["lookup_n"] // 2],
+                           O.mt_keys(seed, case["lookup_n"] - case["lookup_n"] // 2, skip=n)]).astype(np.uint32)
+    assert sha(f.lookup(look)) == case["lookup_sha256"]
+
+
+@pytest.mark.parametrize("q,alpha,seed", [(10, 0.9, 1), (12, 0.5, 2), (14, 0.97, 3), (16, 0.9, 4), (12, 0.99, 5),
+                                          (18, 0.95, 6)])
+def test_rsqf_build_and_batches(gqf, cuda, q, alpha, seed):
+    n = int(alpha * (1 << q))
+    keys = O.mt_keys(seed, n)
+    f = RSQF(gqf, cuda, q)
+    o = O.rsqf_new(q)
+    ret = f.insert(keys)
+    want = O.rsqf_insert_sorted(o, q, keys)
+    assert_same_blocks(f.blocks(), o)
+    assert np.array_equal(ret, want)
+    for k in range(2):  # incremental batches (order-sensitive reference code)
+        b = O.mt_keys(seed + 10 + k, max(64, n // 16))
+        ret = f.insert(b)
+        want = O.rsqf_insert_sorted(o, q, b)
+        assert_same_blocks(f.blocks(), o)
+        assert np.array_equal(ret, want)
+    look = np.concatenate([keys[: n // 2], O.mt_keys(seed + 20, n // 2)])
+    want = O.rsqf_lookup(o, q, look)
+    assert np.array_equal(f.lookup(look, sorted_=True), want)
+    assert np.array_equal(f.lookup(look, sorted_=False), want)
+
+
+def test_rsqf_duplicates_and_empty_batch(gqf, cuda):
+    q = 12
+    keys = O.mt_keys(7, 1500)
+    keys = np.concatenate([keys, keys[:300], keys[:50]])  # RSQF stores duplicates
+    f = RSQF(gqf, cuda, q)
+    o = O.rsqf_new(q)
+    assert np.array_equal(f.insert(keys), O.rsqf_insert_sorted(o, q, keys))
+    assert_same_blocks(f.blocks(), o)
+    assert f.insert(np.zeros(0, np.uint32)).size == 0
+    assert_same_blocks(f.blocks(), o)
+
+
+def test_rsqf_overfull(gqf, cuda):
+    """Past capacity the reference returns -1 for the items it cannot place."""
+    q = 8
+    keys = O.mt_keys(9, 400)  # 256 quotients + 64 spare slots
+    f = RSQF(gqf, cuda, q)
+    o = O.rsqf_new(q)
+    ret = f.insert(keys)
+    want = O.rsqf_insert_sorted(o, q, keys)
+    assert (want < 0).any()
+    assert np.array_equal(ret, want)
+    assert_same_blocks(f.blocks(), o)
