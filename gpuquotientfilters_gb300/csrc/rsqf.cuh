@@ -194,10 +194,36 @@ struct RsqfGroupTable {
     __device__ __forceinline__ uint32_t off(uint32_t b) const { return rd(b)[0]; }
     __device__ __forceinline__ uint64_t occ(uint32_t b) const { return ld_u64_unaligned(rd(b) + 1); }
     __device__ __forceinline__ uint64_t re(uint32_t b) const { return ld_u64_unaligned(rd(b) + 9); }
+    // Remainder fields are addressed as the reference does: bit 5s past
+    // block b's remainder words, which for s >= 64 (reachable through an
+    // offset byte above 64) runs into the following blocks.  Bytes past the
+    // last (guard) block are read as zero and never written; the reference
+    // reads and writes outside its block array there.
+    __device__ __forceinline__ size_t rem_byte(uint32_t b, uint32_t s) const
+    {
+        return (size_t)b * RSQF_BB + 17 + ((size_t)s * RSQF_R >> 3);
+    }
+    __device__ __forceinline__ uint32_t byte_at(size_t a) const
+    {
+        if (a >= (size_t)(nblocks + 1) * RSQF_BB) return 0u;
+        uint32_t b = (uint32_t)(a / RSQF_BB);
+        return (b >= glo && b < ghi) ? t[a] : t0[a];
+    }
     __device__ __forceinline__ uint32_t rem(uint32_t b, uint32_t s) const
     {
-        uint32_t bit = s * RSQF_R;
-        return (uint32_t)(ld_u64_unaligned(rd(b) + 17 + (bit >> 3)) >> (bit & 7)) & 31u;
+        size_t a = rem_byte(b, s);
+        uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);
+        return (w >> ((s * RSQF_R) & 7)) & 31u;
+    }
+    __device__ __forceinline__ void set_byte(size_t a, uint32_t v)
+    {
+        if (a >= (size_t)(nblocks + 1) * RSQF_BB) return;
+        uint32_t b = (uint32_t)(a / RSQF_BB);
+        if (b < glo || b >= ghi) {
+            crossed = true;
+            return;
+        }
+        t[a] = (uint8_t)v;
     }
     __device__ __forceinline__ void set_off(uint32_t b, uint32_t v)
     {
@@ -216,17 +242,19 @@ struct RsqfGroupTable {
     }
     __device__ __forceinline__ void set_rem(uint32_t b, uint32_t s, uint32_t val)
     {
-        uint8_t *p = wr(b);
-        if (!p) return;
-        uint32_t bit = s * RSQF_R;
-        uint8_t *q = p + 17 + (bit >> 3);
-        uint32_t sh = bit & 7;
-        uint32_t w = (uint32_t)q[0] | ((uint32_t)q[1] << 8);  // a field spans at most 2 bytes
+        size_t a = rem_byte(b, s);
+        uint32_t sh = (s * RSQF_R) & 7;
+        uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);  // a field spans at most 2 bytes
         w = (w & ~(31u << sh)) | ((val & 31u) << sh);
-        q[0] = (uint8_t)w;
-        if (sh > 3) q[1] = (uint8_t)(w >> 8);
+        set_byte(a, w & 0xFFu);
+        if (sh > 3) set_byte(a + 1, (w >> 8) & 0xFFu);
     }
 };
+
+// bit s of a 64-bit field; slot indices >= 64 wrap modulo 64 as the
+// reference's `1ULL << slotNumber` does on the CPUs it runs on
+__device__ __forceinline__ uint64_t bit64(uint32_t s) { return 1ull << (s & 63u); }
+__device__ __forceinline__ bool has_bit(uint64_t x, uint32_t s) { return (x >> (s & 63u)) & 1ull; }
 
 // findFirstUnusedSlot (RSQF.cpp:341-365; RSQF.cu:565-590), rank == 0 case
 // included as written there.
@@ -279,9 +307,9 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
         end = select64(f.re((uint32_t)bn) & ~lowmask64(off), rank);
     }
     if (((uint32_t)bn * RSQF_SPB + end < (uint32_t)home * RSQF_SPB + hs) | (off + rank == 0)) {
-        f.set_re((uint32_t)home, re | (1ull << hs));
+        f.set_re((uint32_t)home, re | bit64(hs));
         f.set_rem((uint32_t)home, hs, fr);
-        f.set_occ((uint32_t)home, occ | (1ull << hs));
+        f.set_occ((uint32_t)home, occ | bit64(hs));
         return (int32_t)((uint32_t)home * RSQF_SPB + hs);
     }
     end++;
@@ -302,20 +330,20 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
             const uint32_t ns = RSQF_SPB - 1;
             f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)nb, ns));
             uint64_t r2 = f.re((uint32_t)bn);
-            f.set_re((uint32_t)bn, ((f.re((uint32_t)nb) >> ns) & 1ull) ? (r2 | 1ull) : (r2 & ~1ull));
+            f.set_re((uint32_t)bn, has_bit(f.re((uint32_t)nb), ns) ? (r2 | 1ull) : (r2 & ~1ull));
             unused = RSQF_SPB - 1;
             bn--;
         } else {
             f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)bn, unused - 1));
             uint64_t r2 = f.re((uint32_t)bn);
-            f.set_re((uint32_t)bn, ((r2 >> (unused - 1)) & 1ull) ? (r2 | (1ull << unused)) : (r2 & ~(1ull << unused)));
+            f.set_re((uint32_t)bn, has_bit(r2, unused - 1) ? (r2 | bit64(unused)) : (r2 & ~bit64(unused)));
             unused--;
         }
     }
-    if (!((f.occ((uint32_t)home) >> hs) & 1ull)) {
+    if (!has_bit(f.occ((uint32_t)home), hs)) {
         f.set_rem((uint32_t)bn, unused, fr);
-        f.set_re((uint32_t)bn, f.re((uint32_t)bn) | (1ull << unused));
-        f.set_occ((uint32_t)home, f.occ((uint32_t)home) | (1ull << hs));
+        f.set_re((uint32_t)bn, f.re((uint32_t)bn) | bit64(unused));
+        f.set_occ((uint32_t)home, f.occ((uint32_t)home) | bit64(hs));
         return (int32_t)((uint32_t)bn * RSQF_SPB + unused);
     }
     uint32_t ns = unused - 1;
@@ -325,8 +353,8 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
         nb = bn - 1;
         if (nb < 0) return -1;
     }
-    f.set_re((uint32_t)bn, f.re((uint32_t)bn) | (1ull << unused));
-    f.set_re((uint32_t)nb, f.re((uint32_t)nb) & ~(1ull << ns));
+    f.set_re((uint32_t)bn, f.re((uint32_t)bn) | bit64(unused));
+    f.set_re((uint32_t)nb, f.re((uint32_t)nb) & ~bit64(ns));
     uint32_t nrem = f.rem((uint32_t)nb, ns);
     for (;;) {
         if (f.crossed) return -1;
@@ -354,7 +382,7 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
             ns = unused - 1;
         }
         nrem = f.rem((uint32_t)nb, ns);
-        if (((f.re((uint32_t)nb) >> ns) & 1ull) || (uint32_t)nb * RSQF_SPB + ns < fq) break;
+        if (has_bit(f.re((uint32_t)nb), ns) || (uint32_t)nb * RSQF_SPB + ns < fq) break;
     }
     f.set_rem((uint32_t)bn, unused, fr);
     return (int32_t)((uint32_t)bn * RSQF_SPB + unused);

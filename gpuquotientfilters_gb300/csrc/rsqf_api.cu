@@ -84,7 +84,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_bucket_sort(uint32_t *items, c
     __syncthreads();
     // exclusive scan of the packed u16 counters, S/2 words in skewed order
     {
-        const uint32_t per = (S + SORT_THREADS - 1) / SORT_THREADS;  // quotients per thread (even or 1)
+        // quotients per thread, even so the two u16 counters of a word
+        // belong to one thread
+        const uint32_t per = max(2u, ((S + SORT_THREADS - 1) / SORT_THREADS + 1) & ~1u);
         const uint32_t q0 = min(S, threadIdx.x * per), q1 = min(S, q0 + per);
         uint32_t sum = 0;
         for (uint32_t x = q0; x < q1; x++) sum += cnt16_get(s_cnt, x);

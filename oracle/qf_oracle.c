@@ -516,37 +516,43 @@ static uint64_t lowmask(uint32_t n) { return n >= 64 ? ~0ull : ((1ull << n) - 1u
 
 /* getRemainderGPU / setRemainderGPU, RSQF.cu:91-125: rbits-wide fields,
  * slot s at bit s*rbits of the remainders[] words, spilling into the next
- * word when it crosses a 64-bit boundary. */
+ * word when it crosses a 64-bit boundary.  Slots >= 64 (reachable when an
+ * offset byte exceeds 64) address bytes of the following blocks, as the
+ * reference's word indexing does in its packed array; bytes past the guard
+ * block read as zero and are not written (the reference accesses memory
+ * outside its block array there). */
+static size_t table_end(const rsqf_t *f) { return (size_t)(f->nblocks + 1) * f->bb; }
+
 static uint32_t get_rem(const rsqf_t *f, uint32_t b, uint32_t s)
 {
-    uint32_t bit = s * f->rbits;
-    uint32_t w = bit / 64, sb = bit % 64;
-    const uint8_t *rp = blk(f, b) + 17;
-    uint64_t lo = ld64(rp + 8 * w) >> sb;
-    if (sb + f->rbits > 64) lo |= ld64(rp + 8 * (w + 1)) << (64 - sb);
-    return (uint32_t)(lo & lowmask(f->rbits));
+    uint64_t bit = (uint64_t)s * f->rbits;
+    size_t a = (size_t)b * f->bb + 17 + (size_t)(bit >> 3);
+    uint32_t sh = (uint32_t)(bit & 7);
+    uint32_t v = 0;
+    for (uint32_t k = 0; k < 3; k++)
+        if (a + k < table_end(f)) v |= (uint32_t)f->base[a + k] << (8 * k);
+    return (v >> sh) & (uint32_t)lowmask(f->rbits);
 }
 
-static void set_rem(const rsqf_t *f, uint32_t b, uint32_t s, uint32_t v)
+static void set_rem(const rsqf_t *f, uint32_t b, uint32_t s, uint32_t val)
 {
-    uint32_t bit = s * f->rbits;
-    uint32_t w = bit / 64, sb = bit % 64;
-    uint8_t *rp = blk(f, b) + 17;
-    uint64_t x = ld64(rp + 8 * w);
-    uint32_t first = sb + f->rbits > 64 ? 64 - sb : f->rbits;
-    x &= ~(lowmask(first) << sb);
-    x |= ((uint64_t)v & lowmask(first)) << sb;
-    st64(rp + 8 * w, x);
-    if (first < f->rbits) {
-        uint32_t rest = f->rbits - first;
-        uint64_t y = ld64(rp + 8 * (w + 1));
-        y &= ~lowmask(rest);
-        y |= (uint64_t)v >> first;
-        st64(rp + 8 * (w + 1), y);
-    }
+    uint64_t bit = (uint64_t)s * f->rbits;
+    size_t a = (size_t)b * f->bb + 17 + (size_t)(bit >> 3);
+    uint32_t sh = (uint32_t)(bit & 7);
+    uint32_t v = 0;
+    for (uint32_t k = 0; k < 3; k++)
+        if (a + k < table_end(f)) v |= (uint32_t)f->base[a + k] << (8 * k);
+    uint32_t m = (uint32_t)lowmask(f->rbits) << sh;
+    v = (v & ~m) | ((val << sh) & m);
+    uint32_t nbytes = (sh + f->rbits + 7) / 8;
+    for (uint32_t k = 0; k < nbytes; k++)
+        if (a + k < table_end(f)) f->base[a + k] = (uint8_t)(v >> (8 * k));
 }
 
-static int is_bit(uint64_t x, uint32_t s) { return (int)((x >> s) & 1ull); }
+/* slot indices >= 64 wrap modulo 64, as the reference's 64-bit shifts do on
+ * the CPUs it runs on (x86-64 and AArch64 mask the shift count) */
+static int is_bit(uint64_t x, uint32_t s) { return (int)((x >> (s & 63u)) & 1ull); }
+static uint64_t bit_of(uint32_t s) { return 1ull << (s & 63u); }
 
 /* rankBit, RSQF.cpp:189-193: ones in bits [0, index] */
 static uint32_t rank_bit(uint64_t x, uint32_t index)
@@ -660,9 +666,9 @@ static int32_t rsqf_insert(const rsqf_t *f, uint32_t q, uint32_t fp)
         end = select_bit(get_re(f, (uint32_t)bn) & ~lowmask(off), rank);
     }
     if ((gslot((uint32_t)bn, end) < gslot((uint32_t)home, hs)) | (off + rank == 0)) {
-        set_re(f, (uint32_t)home, re | (1ull << hs));
+        set_re(f, (uint32_t)home, re | bit_of(hs));
         set_rem(f, (uint32_t)home, hs, fr);
-        set_occ(f, (uint32_t)home, occ | (1ull << hs));
+        set_occ(f, (uint32_t)home, occ | bit_of(hs));
         return (int32_t)gslot((uint32_t)home, hs);
     }
     end++;
@@ -682,24 +688,24 @@ static int32_t rsqf_insert(const rsqf_t *f, uint32_t q, uint32_t fp)
             uint32_t ns = SPB - 1;
             set_rem(f, (uint32_t)bn, unused, get_rem(f, (uint32_t)nb, ns));
             if (is_bit(get_re(f, (uint32_t)nb), ns))
-                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | (1ull << unused));
+                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | bit_of(unused));
             else
-                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) & ~(1ull << unused));
+                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) & ~bit_of(unused));
             unused = SPB - 1;
             bn--;
         } else {
             set_rem(f, (uint32_t)bn, unused, get_rem(f, (uint32_t)bn, unused - 1));
             if (is_bit(get_re(f, (uint32_t)bn), unused - 1))
-                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | (1ull << unused));
+                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | bit_of(unused));
             else
-                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) & ~(1ull << unused));
+                set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) & ~bit_of(unused));
             unused--;
         }
     }
     if (!is_bit(get_occ(f, (uint32_t)home), hs)) {
         set_rem(f, (uint32_t)bn, unused, fr);
-        set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | (1ull << unused));
-        set_occ(f, (uint32_t)home, get_occ(f, (uint32_t)home) | (1ull << hs));
+        set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | bit_of(unused));
+        set_occ(f, (uint32_t)home, get_occ(f, (uint32_t)home) | bit_of(hs));
         return (int32_t)gslot((uint32_t)bn, unused);
     }
     uint32_t ns = unused - 1;
@@ -709,8 +715,8 @@ static int32_t rsqf_insert(const rsqf_t *f, uint32_t q, uint32_t fp)
         nb = bn - 1;
         if (nb < 0) return -1;
     }
-    set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | (1ull << unused));
-    set_re(f, (uint32_t)nb, get_re(f, (uint32_t)nb) & ~(1ull << ns));
+    set_re(f, (uint32_t)bn, get_re(f, (uint32_t)bn) | bit_of(unused));
+    set_re(f, (uint32_t)nb, get_re(f, (uint32_t)nb) & ~bit_of(ns));
     uint32_t nrem = get_rem(f, (uint32_t)nb, ns);
     do {
         if (nrem <= fr) {

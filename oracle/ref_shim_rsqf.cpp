@@ -7,14 +7,16 @@
 #include "mt19937ar.h"
 
 extern "C" {
-// Same allocation as initCQF (RSQF.cpp:29-35) plus one zeroed guard block:
-// the reference's `blockNum > numBlocks` bounds checks (RSQF.cpp:351,397)
-// let it touch blocks[numBlocks].
+// Same allocation as initCQF (RSQF.cpp:29-35) plus one zeroed guard block
+// (the reference's `blockNum > numBlocks` bounds checks, RSQF.cpp:351,397,
+// let it touch blocks[numBlocks]) and 64 zeroed padding blocks: at high
+// fill an offset byte above 64 makes its remainder accessors index past the
+// block array, which would otherwise corrupt the heap.
 void *ref_rsqf_new(unsigned q)
 {
     countingQuotientFilter *f = (countingQuotientFilter *)malloc(sizeof(countingQuotientFilter));
     f->qbits = q;
-    f->blocks = (cqf_block *)calloc(calcNumBlocks(q) + 1, sizeof(cqf_block));
+    f->blocks = (cqf_block *)calloc(calcNumBlocks(q) + 1 + 64, sizeof(cqf_block));
     return f;
 }
 void ref_rsqf_free(void *p)

@@ -239,3 +239,32 @@ def test_rsqf_oracle_vs_reference_random_order(q, alpha, seed):
     assert np.array_equal(rb, mine)
     assert np.array_equal(rr, mr)
     assert np.array_equal(lr, O.rsqf_lookup(mine, q, lk))
+
+
+@pytest.mark.skipif(not O.Ref.available(), reason="reference CPU build (oracle/_ref) absent")
+@pytest.mark.parametrize("q,alpha,seed", [(13, 0.97, 42), (16, 0.96, 43), (12, 0.98, 44)])
+def test_rsqf_oracle_vs_reference_sorted_batches(q, alpha, seed):
+    """Sorted batches at high fill (offset bytes above 64 occur): the oracle
+    equals the compiled reference block for block and return for return.
+    Fills stay within capacity: past it the reference's run-end search
+    (RSQF.cpp:444-454) has no bound and reads outside its block array."""
+    import ctypes as C
+    ref = O.Ref()
+    R = ref.rsqf
+    n = int(alpha * (1 << q))
+    f = R.ref_rsqf_new(q)
+    mine = O.rsqf_new(q)
+    try:
+        for k, cnt in enumerate([n, n // 100, n // 100]):
+            keys = O.mt_keys(seed + k, cnt)
+            fps = O.aphash(keys, q, 5)
+            order = np.argsort(fps, kind="stable")
+            rr = np.array([R.ref_rsqf_insert(f, int(x)) for x in keys[order]], np.int32)
+            mr = O.rsqf_insert_sorted(mine, q, keys)
+            bb = int(R.ref_rsqf_block_bytes())
+            nb = O.rsqf_num_blocks(q) + 1
+            rb = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)), shape=(nb * bb,)).copy()
+            assert np.array_equal(rr, mr)
+            assert np.array_equal(rb, mine)
+    finally:
+        R.ref_rsqf_free(f)

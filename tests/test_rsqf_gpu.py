@@ -67,9 +67,11 @@ def test_rsqf_golden(gqf, cuda, case):
     assert sha(f.lookup(look)) == case["lookup_sha256"]
 
 
-@pytest.mark.parametrize("q,alpha,seed", [(10, 0.9, 1), (12, 0.5, 2), (14, 0.97, 3), (16, 0.9, 4), (12, 0.99, 5),
-                                          (18, 0.95, 6)])
+@pytest.mark.parametrize("q,alpha,seed", [(10, 0.9, 1), (12, 0.5, 2), (14, 0.9, 3), (16, 0.9, 4), (12, 0.92, 5),
+                                          (18, 0.9, 6), (13, 0.96, 7)])
 def test_rsqf_build_and_batches(gqf, cuda, q, alpha, seed):
+    """Fills stay below capacity (the reference's run-end search has no bound
+    past it, RSQF.cpp:444-454)."""
     n = int(alpha * (1 << q))
     keys = O.mt_keys(seed, n)
     f = RSQF(gqf, cuda, q)
@@ -79,7 +81,7 @@ def test_rsqf_build_and_batches(gqf, cuda, q, alpha, seed):
     assert_same_blocks(f.blocks(), o)
     assert np.array_equal(ret, want)
     for k in range(2):  # incremental batches (order-sensitive reference code)
-        b = O.mt_keys(seed + 10 + k, max(64, n // 16))
+        b = O.mt_keys(seed + 10 + k, max(64, n // 64))
         ret = f.insert(b)
         want = O.rsqf_insert_sorted(o, q, b)
         assert_same_blocks(f.blocks(), o)
@@ -103,7 +105,10 @@ def test_rsqf_duplicates_and_empty_batch(gqf, cuda):
 
 
 def test_rsqf_overfull(gqf, cuda):
-    """Past capacity the reference returns -1 for the items it cannot place."""
+    """Past capacity items that cannot be placed get -1.  (The reference
+    returns -1 on some of these paths and reads outside its block array on
+    others; the engine and the oracle bound every search at the guard
+    block.)"""
     q = 8
     keys = O.mt_keys(9, 400)  # 256 quotients + 64 spare slots
     f = RSQF(gqf, cuda, q)
