@@ -212,13 +212,66 @@ def run_gpu(args, world, rank, local):
     # end to end through the same API from pinned host buffers
     e2e = e2e_step(args, G, torch, dev, stream, c, qf) if not wanted and q == Q else None
     G.freeFilterGPU(qf)
+    del d_keys, d_look, d_ins, d_del, d_out, d_out2
+    rsqf = rsqf_ops(args, G, torch, dev, stream, flush, peak) if args.rsqf and not wanted else None
     return {
         "value": value, "ms_per_step": t_max / args.steps, "per_op": per_op, "clocks": clk,
-        "gpu_launches": int(launches), "peak": peak, "peak_kind": peak_kind, "e2e": e2e,
+        "gpu_launches": int(launches), "peak": peak, "peak_kind": peak_kind, "e2e": e2e, "rsqf": rsqf,
         "roofline": {"bound": "hbm", "kernel": "bulk build pipeline (hash+bucket scatter, bucket layout, fixup)",
                      "achieved": b["alg_GBps"], "peak": peak, "unit": "GB/s", "frac": b["frac_hbm"],
                      "traffic": None, "peak_source": peak_kind},
     }
+
+
+def rsqf_ops(args, G, torch, dev, stream, flush, peak):
+    """The rank-and-select filter at q=26 (RBITS 5, 64-slot blocks): build to
+    0.9 fill by insertGPU of 60,397,976 MT19937 seed-3 keys into an empty
+    filter, 2^24 sorted lookups (50% positive), then 2^20 incremental
+    inserts.  Reported beside the headline, not counted in it."""
+    from gpuquotientfilters_gb300 import workload as W
+    q = args.q
+    n = W.n_keys(q, 0.9, reference_arithmetic=True)
+    n_look, n_ins = N_LOOKUP >> (Q - q), N_INSERT >> (Q - q)
+    keys = G.mt19937(3, n + n_ins)
+    look = W.mixed_lookups(keys[:n], n_look, 3, skip=n + n_ins)
+
+    def dev_u32(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
+
+    d_keys, d_ins, d_look = dev_u32(keys[:n]), dev_u32(keys[n:]), dev_u32(look)
+    d_ret = torch.empty(n, dtype=torch.int32, device=dev)
+    d_out = torch.empty(n_look, dtype=torch.int32, device=dev)
+    rec = {}
+    for it in range(args.warmup + args.steps):
+        cqf = G.initCQFGPU(q)
+        torch.cuda.synchronize(dev)
+        for name, fn in (("rsqf_build", lambda: G.insertGPU(cqf, n, d_keys, d_ret, stream=stream)),
+                         ("rsqf_lookup_sorted", lambda: G.launchLookups(cqf, n_look, d_look, d_out, stream=stream)),
+                         ("rsqf_insert", lambda: G.insertGPU(cqf, n_ins, d_ins, d_ret, stream=stream))):
+            flush.fill_(1)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            fn()
+            ev1.record(stream)
+            ev1.synchronize()
+            if it >= args.warmup:
+                rec.setdefault(name, []).append(ev0.elapsed_time(ev1))
+        G.freeCQFGPU(cqf)
+    nb = G.calcNumBlocksGPU(q)
+    out = {}
+    # build: key in, slot out, one fingerprint permutation, blocks written once;
+    # lookup: key, result, two 32-B sectors of a 57-B block; insert: key,
+    # slot, two sectors read and written
+    for name, cnt, nbytes in (("rsqf_build", n, 16.0 * n + 57.0 * (nb + 1)),
+                              ("rsqf_lookup_sorted", n_look, 72.0 * n_look),
+                              ("rsqf_insert", n_ins, 136.0 * n_ins)):
+        ms = float(np.mean(rec[name]))
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out[name] = {"n": cnt, "ms": round(ms, 4), "mops": round(cnt / ms / 1e3, 1), "alg_GBps": round(gbs, 1),
+                     "frac_hbm": round(gbs / peak, 4)}
+    out["workload"] = "RSQF q=%d RBITS 5: insertGPU of %d keys (0.9 fill, MT19937 seed 3) into an empty filter, " \
+                      "%d sorted lookups, %d incremental inserts" % (q, n, n_look, n_ins)
+    return out
 
 
 def e2e_step(args, G, torch, dev, stream, c, qf):
@@ -325,6 +378,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--q", type=int, default=Q, help="quotient bits (26 = the benchmark workload; smaller "
                     "values scale every batch by 2^(q-26), for profiling small cases)")
+    ap.add_argument("--no-rsqf", dest="rsqf", action="store_false", help="skip the RSQF ops")
     ap.add_argument("--ops", default="", help="comma list of ops to run (build always runs)")
     args = ap.parse_args()
     world, rank, local = dist_init()
@@ -349,7 +403,7 @@ def main():
                    "q": Q, "r": R, "n_keys": N_KEYS, "l2": "flushed (256 MB write) before every op",
                    "parallelism": "replicas x%d" % world},
         "per_op": r["per_op"], "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"],
-        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"],
+        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "rsqf": r["rsqf"],
     }
     print(json.dumps(out), flush=True)
 
