@@ -320,30 +320,38 @@ def e2e_step(args, G, torch, dev, stream, c, qf):
 
 
 # -------------------------------------------------------------- CPU baseline
-CPU_SAMPLE = dict(n_build=8 << 20, n_lookup=4 << 20, n_insert=1 << 20, n_delete=1 << 20)
+# The whole step (about 20 s on one core).
+CPU_SAMPLE = dict(q=Q, n_build=N_KEYS, n_lookup=N_LOOKUP, n_insert=N_INSERT, n_delete=N_DELETE)
+# The reference arm's per-step sample: the same step on a q=24 filter at the
+# same 0.8 fill (every count divided by 4), so K + W steps end in about a
+# minute.
+REF_SAMPLE = dict(q=24, n_build=13421773, n_lookup=N_LOOKUP >> 2, n_insert=N_INSERT >> 2, n_delete=N_DELETE >> 2)
 
 
 def cpu_sample_run(sample=CPU_SAMPLE):
-    """The oracle port (sequential CPU algorithm of the reference's
-    CPU_version, GPU hash) on a bounded sample of the same workload: build by
-    sequential insertItem of the first n_build keys into a q=26 table, then
-    lookups, inserts and deletes.  Returns (M ops/s, seconds, description)."""
+    """The oracle port (the sequential algorithm of the reference's
+    CPU_version on the GPU table format and hash) on the workload: build by
+    sequential insertItem of n_build keys into an empty q-bit table, then the
+    lookups (50% present), inserts of fresh keys and deletes of present keys.
+    Returns (M ops/s, seconds, description)."""
     import oracle as O
     from gpuquotientfilters_gb300 import workload as W
+    q = sample["q"]
     keys = O.mt_keys(SEED, sample["n_build"])
-    look = W.mixed_lookups(keys, sample["n_lookup"], SEED, skip=N_KEYS + N_INSERT)
-    ins = O.mt_keys(SEED, sample["n_insert"], skip=N_KEYS)
+    look = W.mixed_lookups(keys, sample["n_lookup"], SEED, skip=sample["n_build"] + sample["n_insert"])
+    ins = O.mt_keys(SEED, sample["n_insert"], skip=sample["n_build"])
     dels = keys[: sample["n_delete"]]
-    t = O.sqf_new(Q, R)
+    t = O.sqf_new(q, R)
     t0 = time.perf_counter()
-    O.sqf_insert(t, Q, R, keys)
-    O.sqf_lookup(t, Q, R, look)
-    O.sqf_insert(t, Q, R, ins)
-    O.sqf_delete(t, Q, R, dels)
+    O.sqf_insert(t, q, R, keys)
+    O.sqf_lookup(t, q, R, look)
+    O.sqf_insert(t, q, R, ins)
+    O.sqf_delete(t, q, R, dels)
     dt = time.perf_counter() - t0
-    nops = sum(sample.values())
-    desc = ("oracle port, 1 thread: insertItem of %d keys into a q=26 r=5 table, %d lookups, %d inserts, "
-            "%d deletes" % (sample["n_build"], sample["n_lookup"], sample["n_insert"], sample["n_delete"]))
+    nops = sample["n_build"] + sample["n_lookup"] + sample["n_insert"] + sample["n_delete"]
+    desc = ("oracle port, 1 thread (the reference CPU algorithm is sequential): insertItem of %d keys into an "
+            "empty q=%d r=5 table, %d lookups, %d inserts, %d deletes"
+            % (sample["n_build"], q, sample["n_lookup"], sample["n_insert"], sample["n_delete"]))
     return nops / dt / 1e6, dt, desc
 
 
@@ -352,7 +360,7 @@ def run_reference(args, world, rank):
         return None
     import oracle as O
     O.build()
-    sample = dict(n_build=2 << 20, n_lookup=1 << 20, n_insert=1 << 18, n_delete=1 << 18)
+    sample = REF_SAMPLE
     for _ in range(args.warmup):
         cpu_sample_run(sample)
     vals, secs = [], 0.0
@@ -364,7 +372,8 @@ def run_reference(args, world, rank):
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "M ops/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "SQF q=26 r=5 fill 0.8 (MT19937 seed 2), CPU sample per step", "sample": sample},
+            "config": {"workload": "SQF r=5 fill 0.8 (MT19937 seed 2): build + lookups + inserts + deletes; per step "
+                                   "the q=24 sample of the q=26 workload (counts / 4)", "sample": sample},
             "cpu_baseline": {"value": value, "unit": "M ops/s", "cores": 1, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": "M ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

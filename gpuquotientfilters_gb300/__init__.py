@@ -23,7 +23,7 @@ RBITS = 5
 SLOTS_PER_BLOCK = 64
 
 (GQF_OK, GQF_ERR_ARG, GQF_ERR_FULL, GQF_ERR_CUDA, GQF_ERR_TIMEOUT, GQF_ERR_NOMEM, GQF_ERR_MISMATCH,
- GQF_ERR_LIMIT) = range(8)
+ GQF_ERR_LIMIT, GQF_ERR_FORMAT, GQF_ERR_IO) = range(10)
 
 
 class GQFError(RuntimeError):
@@ -85,6 +85,16 @@ def _lib():
             "gqf_rsqf_insert": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_rsqf_lookup_sorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_rsqf_lookup_unsorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_sqf_image_bytes": (C.c_size_t, [qfp]),
+            "gqf_rsqf_image_bytes": (C.c_size_t, [cqfp]),
+            "gqf_sqf_save": (i32, [qfp, vp, C.c_size_t, vp]),
+            "gqf_rsqf_save": (i32, [cqfp, vp, C.c_size_t, vp]),
+            "gqf_sqf_load": (i32, [qfp, vp, C.c_size_t]),
+            "gqf_rsqf_load": (i32, [cqfp, vp, C.c_size_t]),
+            "gqf_sqf_save_file": (i32, [qfp, C.c_char_p]),
+            "gqf_rsqf_save_file": (i32, [cqfp, C.c_char_p]),
+            "gqf_sqf_load_file": (i32, [qfp, C.c_char_p]),
+            "gqf_rsqf_load_file": (i32, [cqfp, C.c_char_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -306,3 +316,42 @@ def rsqf_blocks_bytes(cqf):
     host = np.empty(n, np.uint8)
     _memcpy_d2h(host.ctypes.data, cqf.blocks, n)
     return host
+
+
+# ------------------------------------------------------------ serialization
+def saveFilter(qf, path: str) -> None:
+    """Writes the SQF image (64-byte header + slot table) to `path`."""
+    _check(_lib().gqf_sqf_save_file(C.byref(qf), os.fsencode(path)), "gqf_sqf_save_file")
+
+
+def loadFilter(path: str) -> quotient_filter:
+    """A new SQF holding the image at `path` (free with freeFilterGPU)."""
+    qf = quotient_filter()
+    _check(_lib().gqf_sqf_load_file(C.byref(qf), os.fsencode(path)), "gqf_sqf_load_file")
+    return qf
+
+
+def saveCQF(cqf, path: str) -> None:
+    """Writes the RSQF image (64-byte header + packed blocks) to `path`."""
+    _check(_lib().gqf_rsqf_save_file(C.byref(cqf), os.fsencode(path)), "gqf_rsqf_save_file")
+
+
+def loadCQF(path: str) -> countingQuotientFilterGPU:
+    """A new RSQF holding the image at `path` (free with freeCQFGPU)."""
+    cqf = countingQuotientFilterGPU()
+    _check(_lib().gqf_rsqf_load_file(C.byref(cqf), os.fsencode(path)), "gqf_rsqf_load_file")
+    return cqf
+
+
+def filter_image(qf) -> bytes:
+    """The SQF image in memory."""
+    n = int(_lib().gqf_sqf_image_bytes(C.byref(qf)))
+    buf = C.create_string_buffer(n)
+    _check(_lib().gqf_sqf_save(C.byref(qf), buf, n, None), "gqf_sqf_save")
+    return buf.raw
+
+
+def filter_from_image(img: bytes) -> quotient_filter:
+    qf = quotient_filter()
+    _check(_lib().gqf_sqf_load(C.byref(qf), img, len(img)), "gqf_sqf_load")
+    return qf

@@ -128,6 +128,8 @@ const char *gqf_status_string(int st)
     case GQF_ERR_NOMEM: return "workspace allocation failed";
     case GQF_ERR_MISMATCH: return "filters differ in q or r";
     case GQF_ERR_LIMIT: return "request exceeds the no-allocation entry point's fixed scratch (see GQF_NOALLOC_MAX_KEYS, GQF_NOALLOC_MAX_Q)";
+    case GQF_ERR_FORMAT: return "filter image: bad magic, version, geometry, size or checksum";
+    case GQF_ERR_IO: return "filter image file could not be opened, read or written";
     default: return "unknown status";
     }
 }

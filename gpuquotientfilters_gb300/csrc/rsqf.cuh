@@ -179,6 +179,12 @@ struct RsqfGroupTable {
     uint32_t nblocks;
     uint32_t glo, ghi;  // this group's blocks
     bool crossed;
+    bool t0_zero;       // t0 is all zero (a batch into an empty filter)
+    // first block >= b that may be non-zero as this group sees the table
+    __device__ __forceinline__ uint32_t zero_run_end(uint32_t b) const
+    {
+        return (t0_zero && b >= ghi) ? nblocks + 1 : b;
+    }
     __device__ __forceinline__ const uint8_t *rd(uint32_t b) const
     {
         return (b >= glo && b < ghi) ? t + (size_t)b * RSQF_BB : t0 + (size_t)b * RSQF_BB;
@@ -249,6 +255,10 @@ struct RsqfGroupTable {
         set_byte(a, w & 0xFFu);
         if (sh > 3) set_byte(a + 1, (w >> 8) & 0xFFu);
     }
+    // The shift loop of the insert (RSQF.cpp:454-476): moves remainders and
+    // runEnd bits one slot up from (bn, unused) down to (re_block, end).
+    // Returns false when a write left the group.
+    __device__ inline bool shift_up(int &bn, uint32_t &unused, int re_block, uint32_t end);
 };
 
 // bit s of a 64-bit field; slot indices >= 64 wrap modulo 64 as the
@@ -256,9 +266,39 @@ struct RsqfGroupTable {
 __device__ __forceinline__ uint64_t bit64(uint32_t s) { return 1ull << (s & 63u); }
 __device__ __forceinline__ bool has_bit(uint64_t x, uint32_t s) { return (x >> (s & 63u)) & 1ull; }
 
+// slot-by-slot shift, exactly as the reference loop runs it
+template <typename Tab>
+__device__ __forceinline__ bool rsqf_shift_serial(Tab &f, int &bn, uint32_t &unused, int re_block, uint32_t end)
+{
+    while ((uint32_t)bn * RSQF_SPB + unused > (uint32_t)re_block * RSQF_SPB + end) {
+        if (f.crossed) return false;
+        if (unused == 0) {
+            const int nb = bn - 1;
+            const uint32_t ns = RSQF_SPB - 1;
+            f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)nb, ns));
+            uint64_t r2 = f.re((uint32_t)bn);
+            f.set_re((uint32_t)bn, has_bit(f.re((uint32_t)nb), ns) ? (r2 | 1ull) : (r2 & ~1ull));
+            unused = RSQF_SPB - 1;
+            bn--;
+        } else {
+            f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)bn, unused - 1));
+            uint64_t r2 = f.re((uint32_t)bn);
+            f.set_re((uint32_t)bn, has_bit(r2, unused - 1) ? (r2 | bit64(unused)) : (r2 & ~bit64(unused)));
+            unused--;
+        }
+    }
+    return !f.crossed;
+}
+
+__device__ inline bool RsqfGroupTable::shift_up(int &bn, uint32_t &unused, int re_block, uint32_t end)
+{
+    return rsqf_shift_serial(*this, bn, unused, re_block, end);
+}
+
 // findFirstUnusedSlot (RSQF.cpp:341-365; RSQF.cu:565-590), rank == 0 case
 // included as written there.
-__device__ inline uint32_t rsqf_first_unused(RsqfGroupTable &f, int &bn, uint32_t start)
+template <typename Tab>
+__device__ inline uint32_t rsqf_first_unused(Tab &f, int &bn, uint32_t start)
 {
     uint32_t cur = start;
     uint64_t occ = f.occ((uint32_t)bn), re = f.re((uint32_t)bn);
@@ -285,8 +325,10 @@ __device__ inline uint32_t rsqf_first_unused(RsqfGroupTable &f, int &bn, uint32_
 }
 
 // insert (RSQF.cpp:367-520 = RSQF.cu:645-875 per item): slot or -1.  On a
-// crossing f.crossed is set and the return value is meaningless.
-__device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp)
+// crossing f.crossed is set and the return value is meaningless.  Tab is
+// the table accessor (per-thread global memory, or a warp's staged blocks).
+template <typename Tab>
+__device__ inline int32_t rsqf_insert(Tab &f, uint32_t q, uint32_t fp)
 {
     const uint32_t fq = (fp >> RSQF_R) & ((1u << q) - 1u);
     const uint32_t fr = fp & 31u;
@@ -304,6 +346,15 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
         off = (int)off - (int)RSQF_SPB > 0 ? off - RSQF_SPB : 0u;
         bn++;
         if ((uint32_t)bn > f.nblocks) return -1;  // past the guard block (the reference reads beyond)
+        if (rank > 0) {
+            // all-zero blocks leave rank unchanged and end unfound: jump them
+            const uint32_t z = f.zero_run_end((uint32_t)bn);
+            for (uint32_t k = (uint32_t)bn; k < z && off; k++) off = (int)off - (int)RSQF_SPB > 0 ? off - RSQF_SPB : 0u;
+            if (z > (uint32_t)bn) {
+                if (z > f.nblocks) return -1;
+                bn = (int)z;
+            }
+        }
         end = select64(f.re((uint32_t)bn) & ~lowmask64(off), rank);
     }
     if (((uint32_t)bn * RSQF_SPB + end < (uint32_t)home * RSQF_SPB + hs) | (off + rank == 0)) {
@@ -323,23 +374,7 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
     if (unused == RSQF_NONE) return -1;
     if (bn > home)
         for (int i = 0; i < bn - home; i++) f.set_off((uint32_t)(bn - i), f.off((uint32_t)(bn - i)) + 1u);
-    while ((uint32_t)bn * RSQF_SPB + unused > (uint32_t)re_block * RSQF_SPB + end) {
-        if (f.crossed) return -1;
-        if (unused == 0) {
-            const int nb = bn - 1;
-            const uint32_t ns = RSQF_SPB - 1;
-            f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)nb, ns));
-            uint64_t r2 = f.re((uint32_t)bn);
-            f.set_re((uint32_t)bn, has_bit(f.re((uint32_t)nb), ns) ? (r2 | 1ull) : (r2 & ~1ull));
-            unused = RSQF_SPB - 1;
-            bn--;
-        } else {
-            f.set_rem((uint32_t)bn, unused, f.rem((uint32_t)bn, unused - 1));
-            uint64_t r2 = f.re((uint32_t)bn);
-            f.set_re((uint32_t)bn, has_bit(r2, unused - 1) ? (r2 | bit64(unused)) : (r2 & ~bit64(unused)));
-            unused--;
-        }
-    }
+    if (!f.shift_up(bn, unused, re_block, end)) return -1;
     if (!has_bit(f.occ((uint32_t)home), hs)) {
         f.set_rem((uint32_t)bn, unused, fr);
         f.set_re((uint32_t)bn, f.re((uint32_t)bn) | bit64(unused));
@@ -387,5 +422,180 @@ __device__ inline int32_t rsqf_insert(RsqfGroupTable &f, uint32_t q, uint32_t fp
     f.set_rem((uint32_t)bn, unused, fr);
     return (int32_t)((uint32_t)bn * RSQF_SPB + unused);
 }
+
+// ----------------------------------------------------------------------------
+// Warp-cooperative accessor: one warp replays one group whose blocks are
+// staged in shared memory, 64 bytes per block with aligned fields (+0
+// offset, +8 occupieds, +16 runEnds, +24 remainders[5]).  All 32 lanes run
+// the insert redundantly on identical data; lane 0 writes, and the shift
+// loop, the one long loop of an insert into a long cluster, moves runEnd
+// bits and remainder fields a word per lane.  Remainder slots >= 64 keep the
+// reference's flat byte addressing through a map from packed byte offsets
+// to the staged layout.  Blocks right of the group are read from t0.
+// ----------------------------------------------------------------------------
+constexpr uint32_t RSQF_SB = 64;  // staged bytes per block
+
+struct RsqfWarpTable {
+    uint8_t *sm;        // staged blocks [glo, ghi)
+    const uint8_t *t0;  // packed table before the batch
+    uint32_t nblocks, glo, ghi;
+    bool crossed;
+    uint32_t lane;
+    bool t0_zero;       // t0 is all zero (a batch into an empty filter)
+
+    __device__ __forceinline__ uint32_t zero_run_end(uint32_t b) const
+    {
+        return (t0_zero && b >= ghi) ? nblocks + 1 : b;
+    }
+
+    __device__ __forceinline__ bool in(uint32_t b) const { return b >= glo && b < ghi; }
+    __device__ __forceinline__ uint8_t *sb(uint32_t b) const { return sm + (size_t)(b - glo) * RSQF_SB; }
+    __device__ __forceinline__ uint64_t &w64(uint32_t b, uint32_t byte) const
+    {
+        return *reinterpret_cast<uint64_t *>(sb(b) + byte);
+    }
+    __device__ __forceinline__ uint32_t off(uint32_t b) const
+    {
+        return in(b) ? sb(b)[0] : t0[(size_t)b * RSQF_BB];
+    }
+    __device__ __forceinline__ uint64_t occ(uint32_t b) const
+    {
+        return in(b) ? w64(b, 8) : ld_u64_unaligned(t0 + (size_t)b * RSQF_BB + 1);
+    }
+    __device__ __forceinline__ uint64_t re(uint32_t b) const
+    {
+        return in(b) ? w64(b, 16) : ld_u64_unaligned(t0 + (size_t)b * RSQF_BB + 9);
+    }
+    // staged address of packed table byte a (its block must be staged)
+    __device__ __forceinline__ uint8_t *staged_byte(size_t a) const
+    {
+        const uint32_t b = (uint32_t)(a / RSQF_BB), j = (uint32_t)(a % RSQF_BB);
+        const uint32_t m = j == 0 ? 0u : (j < 9 ? 8u + (j - 1) : (j < 17 ? 16u + (j - 9) : 24u + (j - 17)));
+        return sb(b) + m;
+    }
+    __device__ __forceinline__ uint32_t byte_at(size_t a) const
+    {
+        if (a >= (size_t)(nblocks + 1) * RSQF_BB) return 0u;
+        const uint32_t b = (uint32_t)(a / RSQF_BB);
+        return in(b) ? *staged_byte(a) : t0[a];
+    }
+    __device__ __forceinline__ uint32_t rem(uint32_t b, uint32_t s) const
+    {
+        if (s < RSQF_SPB && in(b)) {
+            const uint32_t bit = s * RSQF_R, wi = bit >> 6, sh = bit & 63;
+            uint64_t v = w64(b, 24 + 8 * wi) >> sh;
+            if (sh > 59) v |= w64(b, 24 + 8 * (wi + 1)) << (64 - sh);
+            return (uint32_t)v & 31u;
+        }
+        const size_t a = (size_t)b * RSQF_BB + 17 + ((size_t)s * RSQF_R >> 3);
+        const uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);
+        return (w >> ((s * RSQF_R) & 7)) & 31u;
+    }
+    __device__ __forceinline__ bool wr_ok(uint32_t b)
+    {
+        if (!in(b)) {
+            crossed = true;
+            return false;
+        }
+        return true;
+    }
+    __device__ __forceinline__ void set_off(uint32_t b, uint32_t v)
+    {
+        if (wr_ok(b) && lane == 0) sb(b)[0] = (uint8_t)v;
+        __syncwarp();
+    }
+    __device__ __forceinline__ void set_occ(uint32_t b, uint64_t v)
+    {
+        if (wr_ok(b) && lane == 0) w64(b, 8) = v;
+        __syncwarp();
+    }
+    __device__ __forceinline__ void set_re(uint32_t b, uint64_t v)
+    {
+        if (wr_ok(b) && lane == 0) w64(b, 16) = v;
+        __syncwarp();
+    }
+    __device__ __forceinline__ void set_byte(size_t a, uint32_t v)
+    {
+        if (a >= (size_t)(nblocks + 1) * RSQF_BB) return;
+        if (!wr_ok((uint32_t)(a / RSQF_BB))) return;
+        if (lane == 0) *staged_byte(a) = (uint8_t)v;
+        __syncwarp();
+    }
+    __device__ __forceinline__ void set_rem(uint32_t b, uint32_t s, uint32_t val)
+    {
+        if (s < RSQF_SPB) {
+            if (!wr_ok(b)) return;
+            const uint32_t bit = s * RSQF_R, wi = bit >> 6, sh = bit & 63;
+            if (lane == 0) {
+                uint64_t &w = w64(b, 24 + 8 * wi);
+                w = (w & ~(31ull << sh)) | ((uint64_t)(val & 31u) << sh);
+                if (sh > 59) {
+                    uint64_t &w2 = w64(b, 24 + 8 * (wi + 1));
+                    const uint32_t hb = sh + 5 - 64;  // bits in the next word
+                    w2 = (w2 & ~((1ull << hb) - 1)) | ((uint64_t)(val & 31u) >> (5 - hb));
+                }
+            }
+            __syncwarp();
+            return;
+        }
+        const size_t a = (size_t)b * RSQF_BB + 17 + ((size_t)s * RSQF_R >> 3);
+        const uint32_t sh = (s * RSQF_R) & 7;
+        uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);
+        w = (w & ~(31u << sh)) | ((val & 31u) << sh);
+        set_byte(a, w & 0xFFu);
+        if (sh > 3) set_byte(a + 1, (w >> 8) & 0xFFu);
+    }
+
+    // Moves bits [lo, hi) of a group-wide bit array up by k (k < 64): word u
+    // of the array lives at word_at(u); bits outside [lo + k, hi + k) keep
+    // their values.  A word per lane, top words first, reads before writes.
+    template <typename WordAt>
+    __device__ __forceinline__ void move_bits_up(uint64_t lo, uint64_t hi, uint32_t k, WordAt word_at)
+    {
+        const uint64_t dlo = lo + k, dhi = hi + k;  // destination [dlo, dhi)
+        const int64_t ulo = (int64_t)(dlo >> 6), uhi = (int64_t)((dhi - 1) >> 6);
+        for (int64_t top = uhi; top >= ulo; top -= 32) {
+            const int64_t u = top - (int64_t)lane;
+            const bool act = u >= ulo;
+            uint64_t nw = 0;
+            if (act) {
+                const uint64_t cur = *word_at((uint64_t)u);
+                const uint64_t prev = u > 0 ? *word_at((uint64_t)u - 1) : 0ull;
+                const uint64_t sh = (cur << k) | (k ? (prev >> (64 - k)) : 0ull);
+                const uint64_t b0 = (uint64_t)u * 64;
+                const uint64_t m_lo = dlo > b0 ? dlo - b0 : 0, m_hi = dhi < b0 + 64 ? dhi - b0 : 64;
+                const uint64_t mask = (m_hi >= 64 ? ~0ull : ((1ull << m_hi) - 1)) & ~((1ull << m_lo) - 1);
+                nw = (cur & ~mask) | (sh & mask);
+            }
+            __syncwarp();
+            if (act) *word_at((uint64_t)u) = nw;
+            __syncwarp();
+        }
+    }
+
+    // The insert's shift loop.  Within the group and below slot index 64 (the
+    // regular case) it moves the whole range at once: runEnd bits by one
+    // position, remainder fields by five bits; otherwise it runs the
+    // reference loop slot by slot.
+    __device__ inline bool shift_up(int &bn, uint32_t &unused, int re_block, uint32_t end)
+    {
+        const uint64_t sa = (uint64_t)re_block * RSQF_SPB + end, sb_ = (uint64_t)bn * RSQF_SPB + unused;
+        if (sb_ <= sa) return !crossed;
+        if (unused >= RSQF_SPB || end >= RSQF_SPB || !in((uint32_t)bn) || !in((uint32_t)re_block))
+            return rsqf_shift_serial(*this, bn, unused, re_block, end);
+        // group-relative slots [sa, sb_) move to [sa + 1, sb_ + 1)
+        const uint64_t ga = sa - (uint64_t)glo * RSQF_SPB, gb = sb_ - (uint64_t)glo * RSQF_SPB;
+        uint8_t *base = sm;
+        move_bits_up(ga, gb, 1, [base](uint64_t u) {  // runEnds: one word per block
+            return reinterpret_cast<uint64_t *>(base + u * RSQF_SB + 16);
+        });
+        move_bits_up(ga * RSQF_R, gb * RSQF_R, RSQF_R, [base](uint64_t u) {  // remainders: five words per block
+            return reinterpret_cast<uint64_t *>(base + (u / 5) * RSQF_SB + 24 + (u % 5) * 8);
+        });
+        bn = re_block;
+        unused = end;
+        return true;
+    }
+};
 
 }  // namespace gqf

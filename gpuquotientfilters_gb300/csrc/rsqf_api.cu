@@ -1,10 +1,12 @@
 // C ABI of the rank-and-select quotient filter: host orchestration.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <vector>
 
 #include "host_common.cuh"
 #include "rsqf.cuh"
+#include "rsqf_build.cuh"
 #include "sqf_build.cuh"
 
 namespace gqf {
@@ -62,9 +64,12 @@ __host__ __device__ inline size_t sort_smem_bytes(uint32_t tb, uint32_t cap)
     size_t S = (size_t)1 << tb;
     return 4 * (S / 2 + S / 32 + 8) + 4 * (size_t)cap;
 }
+// With bmax non-null it also stores, per bucket, max(quotient_j - j) over
+// the bucket's items (j = index in the whole sorted array), the input of the
+// canonical-position scan.
 __global__ void __launch_bounds__(SORT_THREADS) k_bucket_sort(uint32_t *items, const uint32_t *base,
                                                              const uint32_t *cnt, uint32_t tb, uint32_t cap,
-                                                             uint32_t *err)
+                                                             uint32_t *err, int32_t *bmax)
 {
     extern __shared__ __align__(16) uint32_t smem_sort[];
     const uint32_t S = 1u << tb;
@@ -73,9 +78,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_bucket_sort(uint32_t *items, c
     __shared__ uint32_t s_warp[33];
     const uint32_t b = blockIdx.x, n = cnt[b];
     const size_t b0 = base[b];
-    if (n <= 1) return;
-    if (n > cap) {
-        if (threadIdx.x == 0) atomicOr(err, DEV_ERR_BUCKET_CAP);
+    if (n <= 1 || n > cap) {
+        if (threadIdx.x == 0) {
+            if (n > cap) atomicOr(err, DEV_ERR_BUCKET_CAP);
+            if (bmax) bmax[b] = n == 1 ? (int32_t)(items[b0] >> RSQF_R) - (int32_t)b0 : INT_MIN;
+        }
         return;
     }
     for (uint32_t i = threadIdx.x; i < S / 2 + S / 32 + 8; i += SORT_THREADS) s_cnt[i] = 0;
@@ -127,52 +134,120 @@ __global__ void __launch_bounds__(SORT_THREADS) k_bucket_sort(uint32_t *items, c
         if (g1 - g0 > 1) small_sort(s_it + g0, g1 - g0);
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += SORT_THREADS) items[b0 + i] = s_it[i];
-}
-
-// blk_start[b] = first sorted index whose home block is >= b (b <= nbl).
-__global__ void k_block_starts(const uint32_t *__restrict__ fps, uint32_t n, uint32_t nbl,
-                               uint32_t *__restrict__ blk_start)
-{
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= nbl; b += gridDim.x * blockDim.x) {
-        uint64_t key = (uint64_t)b * RSQF_SPB << RSQF_R;
-        uint32_t lo = 0, hi = n;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
-            if ((uint64_t)fps[mid] < key) lo = mid + 1;
-            else hi = mid;
-        }
-        blk_start[b] = lo;
+    int32_t m = INT_MIN;
+    for (uint32_t i = threadIdx.x; i < n; i += SORT_THREADS) {
+        const uint32_t v = s_it[i];
+        items[b0 + i] = v;
+        m = max(m, (int32_t)(v >> RSQF_R) - (int32_t)(b0 + i));
+    }
+    if (bmax) {
+        int32_t tot;
+        block_excl_max<SORT_THREADS>(m, reinterpret_cast<int32_t *>(s_warp), tot);
+        if (threadIdx.x == 0) bmax[b] = tot;
     }
 }
 
-// One emulation round: every active group (start[b] && active[b]) restores
-// its blocks from t0 and inserts its items in ascending order.
-__global__ void k_rsqf_round(uint8_t *t, const uint8_t *t0, uint32_t nblocks, uint32_t q, const uint32_t *fps,
-                             const uint32_t *blk_start, const uint8_t *start, uint8_t *active, uint8_t *crossed,
-                             uint32_t *n_crossed, int32_t *ret)
+// Lists this round's groups: every active group start with batch items;
+// groups of at most RSQF_WARP_GROUP_MAX blocks go to the warp list, larger
+// ones to the list replayed by one thread each.
+constexpr uint32_t RSQF_WARP_GROUP_MAX = 224;  // blocks one warp stages (14 KB)
+__global__ void k_rsqf_groups(uint32_t nblocks, const uint8_t *__restrict__ start, uint8_t *__restrict__ active,
+                              const uint32_t *__restrict__ fhome, uint32_t *__restrict__ wlist,
+                              uint32_t *__restrict__ blist, uint32_t *__restrict__ counts)
 {
     const uint32_t total = nblocks + 1;  // logical blocks + guard block
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
         if (!start[b] || !active[b]) continue;
+        active[b] = 0;
         uint32_t e = b + 1;
         while (e < total && !start[e]) e++;
-        // restore this group's blocks
+        if (fhome[min(b, nblocks)] == fhome[min(e, nblocks)]) continue;  // no items: table unchanged
+        if (e - b <= RSQF_WARP_GROUP_MAX) {
+            const uint32_t k = atomicAdd(counts, 1u);
+            wlist[2 * k] = b;
+            wlist[2 * k + 1] = e;
+        } else {
+            const uint32_t k = atomicAdd(counts + 1, 1u);
+            blist[2 * k] = b;
+            blist[2 * k + 1] = e;
+        }
+    }
+}
+
+// One replay round, a warp per listed group: stage the group's blocks from
+// t0, insert its items (fhome: first sorted index homed at or past each
+// block) in ascending order, write the blocks back unless a write left the
+// group (then the group is marked crossed and t is left as it was).
+__global__ void __launch_bounds__(32) k_rsqf_round_warp(uint8_t *__restrict__ t, const uint8_t *__restrict__ t0,
+                                                        uint32_t nblocks, uint32_t q, const uint32_t *__restrict__ fps,
+                                                        const uint32_t *__restrict__ fhome,
+                                                        const uint32_t *__restrict__ wlist,
+                                                        const uint32_t *__restrict__ counts,
+                                                        uint8_t *__restrict__ crossed, uint32_t *n_crossed,
+                                                        int32_t *__restrict__ ret, int t0_zero)
+{
+    __shared__ __align__(16) uint8_t sm[RSQF_WARP_GROUP_MAX * RSQF_SB];
+    const uint32_t lane = threadIdx.x;
+    const uint32_t ng = counts[0];
+    for (uint32_t gi = blockIdx.x; gi < ng; gi += gridDim.x) {
+        const uint32_t b = wlist[2 * gi], e = wlist[2 * gi + 1];
+        for (uint32_t i = lane; i < (e - b) * 8; i += 32) {
+            const uint32_t blk = b + i / 8, w = i % 8;
+            const uint8_t *src = t0 + (size_t)blk * RSQF_BB;
+            uint64_t v;
+            if (w == 0) v = src[0];
+            else if (w == 1) v = ld_u64_unaligned(src + 1);
+            else if (w == 2) v = ld_u64_unaligned(src + 9);
+            else v = ld_u64_unaligned(src + 17 + 8 * (w - 3));
+            *reinterpret_cast<uint64_t *>(sm + (size_t)(blk - b) * RSQF_SB + 8 * w) = v;
+        }
+        __syncwarp();
+        RsqfWarpTable f{sm, t0, nblocks, b, e, false, lane, t0_zero != 0};
+        const uint32_t i0 = fhome[min(b, nblocks)], i1 = fhome[min(e, nblocks)];
+        for (uint32_t i = i0; i < i1; i++) {
+            const int32_t slot = rsqf_insert(f, q, fps[i]);
+            if (f.crossed) break;
+            if (lane == 0) ret[i] = slot;
+        }
+        __syncwarp();
+        if (f.crossed) {
+            if (lane == 0) {
+                crossed[b] = 1;
+                atomicAdd(n_crossed, 1u);
+            }
+        } else {
+            for (uint32_t k = lane; k < (e - b) * RSQF_BB; k += 32) {
+                const size_t a = (size_t)b * RSQF_BB + k;
+                t[a] = *f.staged_byte(a);
+            }
+            if (lane == 0) crossed[b] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// The same round for groups too large to stage: one thread per group,
+// blocks restored from t0 in place.
+__global__ void k_rsqf_round_big(uint8_t *t, const uint8_t *t0, uint32_t nblocks, uint32_t q, const uint32_t *fps,
+                                 const uint32_t *fhome, const uint32_t *blist, const uint32_t *counts,
+                                 uint8_t *crossed, uint32_t *n_crossed, int32_t *ret, int t0_zero)
+{
+    const uint32_t ng = counts[1];
+    for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ng; gi += gridDim.x * blockDim.x) {
+        const uint32_t b = blist[2 * gi], e = blist[2 * gi + 1];
         for (size_t i = (size_t)b * RSQF_BB; i < (size_t)e * RSQF_BB; i++) t[i] = t0[i];
-        RsqfGroupTable f{t, t0, nblocks, b, e, false};
-        const uint32_t nbl_items = (nblocks - 1);  // blocks that can be homes
-        const uint32_t i0 = blk_start[min(b, nbl_items)], i1 = blk_start[min(e, nbl_items)];
+        RsqfGroupTable f{t, t0, nblocks, b, e, false, t0_zero != 0};
+        const uint32_t i0 = fhome[min(b, nblocks)], i1 = fhome[min(e, nblocks)];
         bool cross = false;
         for (uint32_t i = i0; i < i1; i++) {
-            int32_t s = rsqf_insert(f, q, fps[i]);
+            const int32_t slot = rsqf_insert(f, q, fps[i]);
             if (f.crossed) {
                 cross = true;
                 break;
             }
-            ret[i] = s;
+            ret[i] = slot;
         }
         crossed[b] = cross ? 1 : 0;
-        active[b] = 0;
         if (cross) atomicAdd(n_crossed, 1u);
     }
 }
@@ -304,10 +379,41 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, i
     return call_end(ar, s, ms);
 }
 
-// insertGPU (RSQF.cu:882-988).  The batch is sorted, then the reference's
-// sequential insert is replayed group by group (see k_rsqf_round); groups
-// whose inserts spill past their last block are merged with their successor
-// and replayed from the pre-batch table until no group spills.
+// insertGPU (RSQF.cu:882-988): the batch is hashed and sorted, then applied
+// in ascending order with the reference's sequential insert semantics.
+//  * Empty filter: blocks written from the canonical positions
+//    (k_rsqf_positions, k_rsqf_assemble); clusters holding a block whose
+//    offset exceeds 62 are then replayed exactly (see rsqf_build.cuh).
+//  * Non-empty filter (or a batch past capacity): groups of blocks split at
+//    estimated pending-shift boundaries are replayed in parallel
+//    (k_rsqf_round); a group whose writes leave it is merged with its
+//    successor and replayed from the pre-batch table until none does.
+// Return slots are indexed by sorted position, as the reference's are.
+static int rsqf_replay_rounds(uint8_t *t, const uint8_t *t0, uint32_t nbl, uint32_t q, const uint32_t *items,
+                              const uint32_t *fhome, uint8_t *start, uint8_t *active, uint8_t *crossed,
+                              uint32_t *wlist, uint32_t *blist, uint32_t *ctr, int32_t *d_ret, bool t0_zero,
+                              cudaStream_t s)
+{
+    const DeviceInfo &di = device_info(current_device());
+    const uint32_t grid = std::min<uint32_t>((nbl + 1 + 255) / 256, di.sms * 8);
+    for (int round = 0;; round++) {
+        GQF_CK(cudaMemsetAsync(ctr, 0, 3 * sizeof(uint32_t), s));  // warp list, big list, crossed
+        k_rsqf_groups<<<grid, 256, 0, s>>>(nbl, start, active, fhome, wlist, blist, ctr);
+        k_rsqf_round_warp<<<di.sms * 16, 32, 0, s>>>(t, t0, nbl, q, items, fhome, wlist, ctr, crossed, ctr + 2,
+                                                     d_ret, t0_zero ? 1 : 0);
+        k_rsqf_round_big<<<std::max(1, di.sms), 64, 0, s>>>(t, t0, nbl, q, items, fhome, blist, ctr, crossed,
+                                                             ctr + 2, d_ret, t0_zero ? 1 : 0);
+        count_launches(3);
+        uint32_t h_n = 0;
+        GQF_CK(cudaMemcpyAsync(&h_n, ctr + 2, 4, cudaMemcpyDeviceToHost, s));
+        GQF_CK(cudaStreamSynchronize(s));
+        if (h_n == 0) return GQF_OK;
+        if (round > 100000) return GQF_ERR_TIMEOUT;
+        k_rsqf_merge<<<grid, 256, 0, s>>>(nbl, start, active, crossed);
+        count_launches(1);
+    }
+}
+
 int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_ret, void *stream, float *ms)
 {
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_ret))) return GQF_ERR_ARG;
@@ -315,63 +421,91 @@ int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t 
     const uint32_t q = cqf->qbits, nbl = cqf->numBlocks;
     const BucketGeom g = rsqf_geom(q, (uint64_t)n);
     const size_t tbytes = rsqf_table_bytes(nbl);
+    const uint32_t ntiles = (nbl + 1 + PEND_TILE - 1) / PEND_TILE;
+    uint8_t *table = static_cast<uint8_t *>(cqf->blocks);
     Arena &ar = arena(current_device());
     std::lock_guard<std::mutex> lk(ar.mu);
     Sizer z;
     z.take<uint32_t>(g.nb);
     z.take<uint32_t>(g.nb + 1);
     z.take<uint32_t>(std::max(n, 1));
-    z.take<uint32_t>(nbl + 2);
+    z.take<int32_t>(g.nb);
+    z.take<int32_t>(g.nb);
+    z.take<uint32_t>(nbl + 1);
+    z.take<uint32_t>(nbl + 1);
     z.take<uint8_t>(tbytes);
-    z.take<uint8_t>(nbl + 1);
-    z.take<uint8_t>(nbl + 1);
-    z.take<uint8_t>(nbl + 1);
-    z.take<uint32_t>(1);
+    for (int k = 0; k < 4; k++) z.take<uint8_t>(nbl + 1);
+    z.take<PendFn>(nbl + 1);
+    z.take<PendFn>(ntiles);
+    z.take<uint32_t>(RCTL_WORDS);
+    z.take<uint32_t>(3);
+    z.take<uint32_t>(2 * (size_t)(nbl + 1));
+    z.take<uint32_t>(2 * (size_t)(nbl + 1));
     void *basep = arena_reserve(ar, z.off);
     if (!basep) return GQF_ERR_NOMEM;
     Carver c(basep);
     uint32_t *cnt = c.take<uint32_t>(g.nb), *base = c.take<uint32_t>(g.nb + 1);
-    uint32_t *items = c.take<uint32_t>(std::max(n, 1)), *blk_start = c.take<uint32_t>(nbl + 2);
-    uint8_t *t0 = c.take<uint8_t>(tbytes), *start = c.take<uint8_t>(nbl + 1), *active = c.take<uint8_t>(nbl + 1),
-            *crossed = c.take<uint8_t>(nbl + 1);
-    uint32_t *ncross = c.take<uint32_t>(1);
+    uint32_t *items = c.take<uint32_t>(std::max(n, 1));
+    int32_t *bmax = c.take<int32_t>(g.nb), *bpre = c.take<int32_t>(g.nb);
+    uint32_t *fpos = c.take<uint32_t>(nbl + 1), *fhome = c.take<uint32_t>(nbl + 1);
+    uint8_t *t0 = c.take<uint8_t>(tbytes);
+    uint8_t *start = c.take<uint8_t>(nbl + 1), *active = c.take<uint8_t>(nbl + 1), *crossed = c.take<uint8_t>(nbl + 1),
+            *sus = c.take<uint8_t>(nbl + 1);
+    PendFn *fn = c.take<PendFn>(nbl + 1), *tile_fn = c.take<PendFn>(ntiles);
+    uint32_t *ctl = c.take<uint32_t>(RCTL_WORDS), *ctr = c.take<uint32_t>(3);
+    uint32_t *wlist = c.take<uint32_t>(2 * (size_t)(nbl + 1)), *blist = c.take<uint32_t>(2 * (size_t)(nbl + 1));
     int st = call_begin(ar, s, true);
     if (st) return st;
     if (n > 0) {
+        const DeviceInfo &di = device_info(current_device());
+        GQF_CK(cudaMemsetAsync(ctl, 0, RCTL_WORDS * 4, s));
+        k_rsqf_nonzero<<<di.sms * 4, 512, 0, s>>>(table, (size_t)(nbl + 1) * RSQF_BB, ctl);
+        count_launches(1);
         st = rsqf_bucket(d_keys, (uint32_t)n, g, items, nullptr, cnt, base, ar.err, s);
         if (st) return st;
-        const uint32_t S = 1u << g.tb;
-        const DeviceInfo &di = device_info(current_device());
         // per-bucket sort: capacity from the largest bucket the smem allows
         size_t maxsm = (size_t)(di.smem_optin > 0 ? di.smem_optin : 99 * 1024) - 2048;
         size_t fixed = sort_smem_bytes(g.tb, 0);
         uint32_t cap = maxsm > fixed ? (uint32_t)std::min<size_t>((maxsm - fixed) / 4, 65535) : 0;
         size_t sm = sort_smem_bytes(g.tb, cap);
         GQF_CK(set_smem(k_bucket_sort, sm));
-        k_bucket_sort<<<g.nb, SORT_THREADS, sm, s>>>(items, base, cnt, g.tb, cap, ar.err);
-        (void)S;
-        k_block_starts<<<(nbl + 2 + 255) / 256, 256, 0, s>>>(items, (uint32_t)n, nbl - 1, blk_start);
-        GQF_CK(cudaMemcpyAsync(t0, cqf->blocks, tbytes, cudaMemcpyDeviceToDevice, s));
-        // initial groups of 4 blocks
-        std::vector<uint8_t> h_start(nbl + 1, 0);
-        for (uint32_t b = 0; b <= nbl; b += 4) h_start[b] = 1;
-        GQF_CK(cudaMemcpyAsync(start, h_start.data(), nbl + 1, cudaMemcpyHostToDevice, s));
-        GQF_CK(cudaMemcpyAsync(active, h_start.data(), nbl + 1, cudaMemcpyHostToDevice, s));
-        GQF_CK(cudaMemsetAsync(crossed, 0, nbl + 1, s));
-        count_launches(2);
-        const uint32_t grid = std::min<uint32_t>((nbl + 1 + 127) / 128, di.sms * 16);
-        for (int round = 0;; round++) {
-            GQF_CK(cudaMemsetAsync(ncross, 0, 4, s));
-            k_rsqf_round<<<grid, 128, 0, s>>>(static_cast<uint8_t *>(cqf->blocks), t0, nbl, q, items, blk_start,
-                                             start, active, crossed, ncross, d_ret);
-            count_launches(1);
-            uint32_t h_n = 0;
-            GQF_CK(cudaMemcpyAsync(&h_n, ncross, 4, cudaMemcpyDeviceToHost, s));
-            GQF_CK(cudaStreamSynchronize(s));
-            if (h_n == 0) break;
-            if (round > 100000) return GQF_ERR_TIMEOUT;
-            k_rsqf_merge<<<grid, 128, 0, s>>>(nbl, start, active, crossed);
-            count_launches(1);
+        k_bucket_sort<<<g.nb, SORT_THREADS, sm, s>>>(items, base, cnt, g.tb, cap, ar.err, bmax);
+        k_rsqf_scan_max<<<1, 1024, 0, s>>>(bmax, g.nb, bpre);
+        k_rsqf_positions<<<g.nb, RPOS_THREADS, 0, s>>>(items, (uint32_t)n, base, cnt, bpre, nbl, nbl * RSQF_SPB,
+                                                       d_ret, fpos, fhome, ctl, ar.err);
+        const uint32_t agrid = std::min<uint32_t>((nbl + 1 + 7) / 8, di.sms * 64);
+        k_rsqf_assemble<<<agrid, 256, 0, s>>>(table, items, d_ret, (uint32_t)n, nbl, fpos, fhome, start, sus, ctl, ar.err);
+        count_launches(4);
+        GQF_CK(cudaGetLastError());
+        uint32_t h_ctl[RCTL_WORDS], h_err = 0;
+        GQF_CK(cudaMemcpyAsync(h_ctl, ctl, sizeof h_ctl, cudaMemcpyDeviceToHost, s));
+        GQF_CK(cudaMemcpyAsync(&h_err, ar.err, sizeof h_err, cudaMemcpyDeviceToHost, s));
+        GQF_CK(cudaStreamSynchronize(s));
+        if (h_err) return dev_err_to_status(h_err);
+        const uint32_t grid = std::min<uint32_t>((nbl + 1 + 255) / 256, di.sms * 16);
+        if (!h_ctl[RCTL_NONEMPTY] && !h_ctl[RCTL_OVER]) {
+            if (h_ctl[RCTL_NSUS]) {
+                // replay the clusters the canonical positions do not describe,
+                // each from its empty blocks
+                GQF_CK(cudaMemsetAsync(t0, 0, tbytes, s));
+                GQF_CK(cudaMemsetAsync(active, 0, nbl + 1, s));
+                GQF_CK(cudaMemsetAsync(crossed, 0, nbl + 1, s));
+                k_rsqf_mark_sus<<<grid, 256, 0, s>>>(nbl, start, sus, active);
+                count_launches(1);
+                st = rsqf_replay_rounds(table, t0, nbl, q, items, fhome, start, active, crossed, wlist, blist, ctr,
+                                        d_ret, true, s);
+                if (st) return st;
+            }
+        } else {
+            GQF_CK(cudaMemcpyAsync(t0, table, tbytes, cudaMemcpyDeviceToDevice, s));
+            RsqfView v0{t0, nbl};
+            k_pend_reduce<<<ntiles, PEND_THREADS, 0, s>>>(v0, nbl, items, fhome, fn, tile_fn);
+            k_pend_scan_tiles<<<1, 32, 0, s>>>(tile_fn, ntiles);
+            k_pend_apply<<<ntiles, PEND_THREADS, 0, s>>>(nbl, fn, tile_fn, start, active, crossed);
+            count_launches(3);
+            st = rsqf_replay_rounds(table, t0, nbl, q, items, fhome, start, active, crossed, wlist, blist, ctr, d_ret,
+                                    false, s);
+            if (st) return st;
         }
     }
     return call_end(ar, s, ms ? ms : nullptr);

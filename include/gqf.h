@@ -31,7 +31,9 @@ typedef enum gqf_status {
     GQF_ERR_TIMEOUT = 4,   /* a bounded device-side wait ran out            */
     GQF_ERR_NOMEM = 5,     /* workspace allocation failed                   */
     GQF_ERR_MISMATCH = 6,  /* mergeTwoFilters on filters of different q/r   */
-    GQF_ERR_LIMIT = 7      /* request larger than the fixed no-allocation scratch */
+    GQF_ERR_LIMIT = 7,     /* request larger than the fixed no-allocation scratch */
+    GQF_ERR_FORMAT = 8,    /* serialized image: bad header, size or checksum */
+    GQF_ERR_IO = 9         /* file could not be opened, read or written */
 } gqf_status;
 
 /* Standard quotient filter handle: identical to `struct quotient_filter`
@@ -154,6 +156,27 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
 /* launchUnsortedLookups, RSQF.cu:540-563 */
 int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
                              int32_t *d_out, void *stream, float *ms);
+
+/* ---------------- serialization (no counterpart in the reference) ------- */
+/* Checkpoint / restore of a filter as one host image: a 64-byte header
+ * (magic "GQFSQF01" or "GQFRSQF1", format version, q, r, payload bytes,
+ * FNV-1a-64 checksum of the payload; little-endian) followed by the raw
+ * device table: the SQF slot array exactly as calcNumSlotsGPU sizes it, or
+ * the RSQF's numBlocks packed 57-byte blocks (the guard block is not
+ * stored).  Images restore bit-identically into a filter of the same q/r. */
+#define GQF_IMAGE_HEADER_BYTES 64
+size_t gqf_sqf_image_bytes(const gqf_sqf *qf);
+size_t gqf_rsqf_image_bytes(const gqf_rsqf *cqf);
+/* copy the filter into host memory `buf` of `cap` bytes (waits for `stream`) */
+int gqf_sqf_save(const gqf_sqf *qf, void *buf, size_t cap, void *stream);
+int gqf_rsqf_save(const gqf_rsqf *cqf, void *buf, size_t cap, void *stream);
+/* allocate a filter (as gqf_sqf_init / gqf_rsqf_init) holding the image */
+int gqf_sqf_load(gqf_sqf *qf, const void *buf, size_t len);
+int gqf_rsqf_load(gqf_rsqf *cqf, const void *buf, size_t len);
+int gqf_sqf_save_file(const gqf_sqf *qf, const char *path);
+int gqf_rsqf_save_file(const gqf_rsqf *cqf, const char *path);
+int gqf_sqf_load_file(gqf_sqf *qf, const char *path);
+int gqf_rsqf_load_file(gqf_rsqf *cqf, const char *path);
 
 #ifdef __cplusplus
 }

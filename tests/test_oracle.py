@@ -268,3 +268,39 @@ def test_rsqf_oracle_vs_reference_sorted_batches(q, alpha, seed):
             assert np.array_equal(rb, mine)
     finally:
         R.ref_rsqf_free(f)
+
+
+def test_rsqf_sorted_build_canonical_below_offset_63():
+    """The engine writes an empty-filter batch from canonical positions
+    wherever every block offset stays <= 62 and replays the rest.  This pins
+    that rule on the oracle (the reference's sequential insert): random
+    fills plus hot quotient ranges; every table whose canonical offsets stay
+    <= 62 equals the canonical layout, and tables with a larger offset
+    generally do not."""
+    rng = np.random.default_rng(7)
+    seen_eq = seen_ne = 0
+    for trial in range(120):
+        q = int(rng.integers(8, 11))
+        fps = [rng.integers(0, (1 << q) << 5, int(rng.uniform(0.3, 0.95) * (1 << q)))]
+        for _ in range(int(rng.integers(0, 4))):
+            k, hot = int(rng.integers(10, 120)), int(rng.integers(0, 1 << q))
+            fps.append((hot << 5) + rng.integers(0, 32, k))
+        fps = np.sort(np.concatenate(fps).astype(np.uint32))
+        i = np.arange(fps.size, dtype=np.int64)
+        qs = (fps >> 5).astype(np.int64)
+        pos = i + np.maximum.accumulate(qs - i)
+        nbl = (1 << q) // 64 + 1
+        if pos[-1] >= nbl * 64:
+            continue
+        off = np.searchsorted(qs, 64 * np.arange(nbl)) - np.searchsorted(pos, 64 * np.arange(nbl))
+        b = O.rsqf_new(q)
+        rets = np.array([O.lib().or_rsqf_insert_fp(b, q, 5, int(f)) for f in fps])
+        c = O.rsqf_new(q)
+        assert O.rsqf_layout_sorted(c, q, fps) == 0
+        same = np.array_equal(b, c) and np.array_equal(rets, pos)
+        if off.max() <= 62:
+            assert same, (trial, q, int(off.max()))
+            seen_eq += 1
+        elif not same:
+            seen_ne += 1
+    assert seen_eq > 30 and seen_ne > 10

@@ -118,3 +118,48 @@ def test_rsqf_overfull(gqf, cuda):
     assert (want < 0).any()
     assert np.array_equal(ret, want)
     assert_same_blocks(f.blocks(), o)
+
+
+@pytest.mark.parametrize("q,seed", [(12, 31), (14, 32), (16, 33)])
+def test_rsqf_long_spills_replayed(gqf, cuda, q, seed):
+    """Hot quotient ranges push block offsets past 62, where the reference's
+    findFirstUnusedSlot departs from the canonical positions: those clusters
+    go through the exact replay, the rest is written from positions."""
+    cand = O.mt_keys(seed, 60 << q >> 6 << 6)
+    fps = O.aphash(cand, q, 5)
+    hot = []
+    for k in range(4):
+        lo = (k + 1) * (1 << q) // 5
+        hot.append(cand[((fps >> 5) >= lo) & ((fps >> 5) < lo + 40)][:150 + 20 * k])
+    keys = np.concatenate([O.mt_keys(seed + 1, int(0.6 * (1 << q)))] + hot)
+    f = RSQF(gqf, cuda, q)
+    o = O.rsqf_new(q)
+    ret = f.insert(keys)
+    want = O.rsqf_insert_sorted(o, q, keys)
+    assert_same_blocks(f.blocks(), o)
+    assert np.array_equal(ret, want)
+    more = np.concatenate([O.mt_keys(seed + 2, 1 << (q - 5)), hot[0][:30]])
+    assert np.array_equal(f.insert(more), O.rsqf_insert_sorted(o, q, more))
+    assert_same_blocks(f.blocks(), o)
+
+
+def test_rsqf_config3_full_size(gqf, cuda):
+    """q=26, 60,397,976 MT19937 seed-3 keys (fill 0.9) into an empty filter:
+    all 59.8 MB of blocks and every return slot identical to the sequential
+    reference semantics; then 2^20 incremental inserts and 2^22 lookups."""
+    from gpuquotientfilters_gb300 import workload as W
+    q = 26
+    n = W.n_keys(q, 0.9, reference_arithmetic=True)
+    keys = O.mt_keys(3, n + (1 << 20))
+    f = RSQF(gqf, cuda, q)
+    o = O.rsqf_new(q)
+    ret = f.insert(keys[:n])
+    want = O.rsqf_insert_sorted(o, q, keys[:n])
+    assert_same_blocks(f.blocks(), o)
+    assert np.array_equal(ret, want)
+    ret = f.insert(keys[n:])
+    want = O.rsqf_insert_sorted(o, q, keys[n:])
+    assert_same_blocks(f.blocks(), o)
+    assert np.array_equal(ret, want)
+    look = W.mixed_lookups(keys[:n], 1 << 22, 3, skip=n + (1 << 20))
+    assert np.array_equal(f.lookup(look), O.rsqf_lookup(o, q, look))
