@@ -214,9 +214,11 @@ def run_gpu(args, world, rank, local):
     G.freeFilterGPU(qf)
     del d_keys, d_look, d_ins, d_del, d_out, d_out2
     rsqf = rsqf_ops(args, G, torch, dev, stream, flush, peak) if args.rsqf and not wanted else None
+    batched = batched_ops(args, G, torch, dev, stream, flush, peak) if args.batched and not wanted else None
     return {
         "value": value, "ms_per_step": t_max / args.steps, "per_op": per_op, "clocks": clk,
         "gpu_launches": int(launches), "peak": peak, "peak_kind": peak_kind, "e2e": e2e, "rsqf": rsqf,
+        "batched": batched,
         "roofline": {"bound": "hbm", "kernel": "bulk build pipeline (hash+bucket scatter, bucket layout, fixup)",
                      "achieved": b["alg_GBps"], "peak": peak, "unit": "GB/s", "frac": b["frac_hbm"],
                      "traffic": None, "peak_source": peak_kind},
@@ -272,6 +274,77 @@ def rsqf_ops(args, G, torch, dev, stream, flush, peak):
     out["workload"] = "RSQF q=%d RBITS 5: insertGPU of %d keys (0.9 fill, MT19937 seed 3) into an empty filter, " \
                       "%d sorted lookups, %d incremental inserts" % (q, n, n_look, n_ins)
     return out
+
+
+def batched_ops(args, G, torch, dev, stream, flush, peak):
+    """256 independent filters (q uniform in [12, 22], fill in [0.5, 0.9],
+    Pareto(1.5) lookup batches, MT19937 seed 4 substreams): every filter
+    bulk built (NoDup) and then queried, (a) as one batch -- one launch per
+    pipeline kernel for all filters, replayed from a CUDA graph, launch shape
+    from the autotuner -- and (b) one bulkBuildSegmentedLayouts +
+    launchUnsortedLookups call per filter.  Both timed with CUDA events on
+    the stream, L2 flushed before each repetition; the tables of (a) and (b)
+    are compared."""
+    from gpuquotientfilters_gb300 import autotune
+    from gpuquotientfilters_gb300 import workload as W
+    c = W.config4()
+
+    def dev_u32(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
+
+    jobs, jobs_ref = [], []
+    for f in c:
+        dk, dl = dev_u32(f["keys"]), dev_u32(f["lookups"])
+        res = torch.empty(f["lookups"].size, dtype=torch.int32, device=dev)
+        jobs.append((G.initFilterGPU(f["q"], 5), dk, dl, res))
+        jobs_ref.append((G.initFilterGPU(f["q"], 5), dk, dl, torch.empty_like(res)))
+    choice, sweep = autotune.tune(G, jobs, True, use_cache=False, cache=None, stream=stream)
+    b = G.Batch(jobs, True, choice["bucket_bits"], choice["scatter_chunk"])
+
+    def timed(fn):
+        out = []
+        for it in range(args.warmup + args.steps):
+            flush.fill_(1)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            fn()
+            ev1.record(stream)
+            ev1.synchronize()
+            if it >= args.warmup:
+                out.append(ev0.elapsed_time(ev1))
+        return float(np.mean(out))
+
+    launches0 = G.lib().gqf_kernel_launches()
+    ms_batch = timed(lambda: b.run(True, stream))
+    batch_launches = (G.lib().gqf_kernel_launches() - launches0) // (args.warmup + args.steps)
+
+    def per_filter():
+        for (qf, dk, dl, res) in jobs_ref:
+            G.bulkBuildSegmentedLayouts(qf, dk.numel(), dk, True, stream=stream)
+            G.launchUnsortedLookups(qf, dl.numel(), dl, res, stream=stream)
+
+    launches0 = G.lib().gqf_kernel_launches()
+    ms_plain = timed(per_filter)
+    plain_launches = (G.lib().gqf_kernel_launches() - launches0) // (args.warmup + args.steps)
+    same = all(torch.equal(j[3], r[3]) for j, r in zip(jobs, jobs_ref)) and all(
+        np.array_equal(G.table_bytes(j[0]), G.table_bytes(r[0])) for j, r in zip(jobs[:16], jobs_ref[:16]))
+    n_keys = sum(f["keys"].size for f in c)
+    n_look = sum(f["lookups"].size for f in c)
+    T = sum(G.calcNumSlotsGPU(f["q"], 5) for f in c)
+    nbytes = 12.0 * n_keys + T + 40.0 * n_look
+    b.close()
+    for j in jobs + jobs_ref:
+        G.freeFilterGPU(j[0])
+    gbs = nbytes / (ms_batch / 1e3) / 1e9
+    return {"workload": "256 SQFs r=5, q U[12,22], fill U[0.5,0.9], NoDup build + Pareto(1.5) lookups in "
+                        "[2^8,2^20] (50% positive), MT19937 seed 4 substreams",
+            "keys": int(n_keys), "lookups": int(n_look),
+            "batched_graph_ms": round(ms_batch, 4), "per_filter_calls_ms": round(ms_plain, 4),
+            "speedup": round(ms_plain / ms_batch, 2), "mops": round((n_keys + n_look) / ms_batch / 1e3, 1),
+            "alg_GBps": round(gbs, 1), "frac_hbm": round(gbs / peak, 4), "tuning": choice,
+            "tuning_sweep_ms": {"%d/%d" % k: round(v, 4) for k, v in sweep.items()},
+            "launches_batched": int(batch_launches), "launches_per_filter": int(plain_launches),
+            "results_identical": bool(same)}
 
 
 def e2e_step(args, G, torch, dev, stream, c, qf):
@@ -388,6 +461,7 @@ def main():
     ap.add_argument("--q", type=int, default=Q, help="quotient bits (26 = the benchmark workload; smaller "
                     "values scale every batch by 2^(q-26), for profiling small cases)")
     ap.add_argument("--no-rsqf", dest="rsqf", action="store_false", help="skip the RSQF ops")
+    ap.add_argument("--no-batched", dest="batched", action="store_false", help="skip the batched-filter ops")
     ap.add_argument("--ops", default="", help="comma list of ops to run (build always runs)")
     args = ap.parse_args()
     world, rank, local = dist_init()
@@ -412,7 +486,7 @@ def main():
                    "q": Q, "r": R, "n_keys": N_KEYS, "l2": "flushed (256 MB write) before every op",
                    "parallelism": "replicas x%d" % world},
         "per_op": r["per_op"], "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"],
-        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "rsqf": r["rsqf"],
+        "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "rsqf": r["rsqf"], "batched": r["batched"],
     }
     print(json.dumps(out), flush=True)
 

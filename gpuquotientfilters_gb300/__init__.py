@@ -38,6 +38,17 @@ class quotient_filter(C.Structure):
                 ("table", C.c_void_p)]
 
 
+class gqf_sqf_job(C.Structure):
+    """One filter of a batch (include/gqf.h): bulk build from n_build keys,
+    then n_lookup unsorted lookups."""
+    _fields_ = [("filter", quotient_filter), ("n_build", C.c_int), ("d_build_keys", C.c_void_p),
+                ("n_lookup", C.c_int), ("d_lookup_keys", C.c_void_p), ("d_results", C.c_void_p)]
+
+
+class gqf_batch_tuning(C.Structure):
+    _fields_ = [("bucket_bits", C.c_int), ("scatter_chunk", C.c_int)]
+
+
 class countingQuotientFilterGPU(C.Structure):
     """struct countingQuotientFilterGPU (RSQF.cuh:32-37)."""
     _fields_ = [("qbits", C.c_uint), ("numBlocks", C.c_uint), ("blocks", C.c_void_p)]
@@ -85,6 +96,11 @@ def _lib():
             "gqf_rsqf_insert": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_rsqf_lookup_sorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_rsqf_lookup_unsorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_batch_create": (i32, [C.POINTER(C.c_void_p), C.POINTER(gqf_sqf_job), i32, i32,
+                                       C.POINTER(gqf_batch_tuning)]),
+            "gqf_batch_run": (i32, [C.c_void_p, i32, vp, f32p]),
+            "gqf_batch_tuning_of": (i32, [C.c_void_p, C.POINTER(gqf_batch_tuning)]),
+            "gqf_batch_destroy": (i32, [C.c_void_p]),
             "gqf_sqf_image_bytes": (C.c_size_t, [qfp]),
             "gqf_rsqf_image_bytes": (C.c_size_t, [cqfp]),
             "gqf_sqf_save": (i32, [qfp, vp, C.c_size_t, vp]),
@@ -355,3 +371,55 @@ def filter_from_image(img: bytes) -> quotient_filter:
     qf = quotient_filter()
     _check(_lib().gqf_sqf_load(C.byref(qf), img, len(img)), "gqf_sqf_load")
     return qf
+
+
+# ------------------------------------------------------------ batched filters
+class Batch:
+    """Many filters built and queried by one launch per pipeline kernel,
+    replayed from a captured CUDA graph (gqf_batch_* in include/gqf.h).
+
+    jobs: sequence of (filter, build_keys or None, lookup_keys or None,
+    results or None); tensors or raw device pointers with lengths taken from
+    the tensors (pass (ptr, n) tuples for raw pointers)."""
+
+    def __init__(self, jobs, no_duplicates=True, bucket_bits=0, scatter_chunk=0):
+        def ptr_len(x):
+            if x is None:
+                return 0, 0
+            if isinstance(x, tuple):
+                return int(x[0]), int(x[1])
+            return int(x.data_ptr()), int(x.numel())
+        arr = (gqf_sqf_job * len(jobs))()
+        self._keep = list(jobs)
+        for i, (qf, bk, lk, res) in enumerate(jobs):
+            bp, bn = ptr_len(bk)
+            lp, ln = ptr_len(lk)
+            rp, _ = ptr_len(res)
+            arr[i] = gqf_sqf_job(qf, bn, bp, ln, lp, rp)
+        tune = gqf_batch_tuning(int(bucket_bits), int(scatter_chunk))
+        h = C.c_void_p()
+        _check(_lib().gqf_batch_create(C.byref(h), arr, len(jobs), int(bool(no_duplicates)), C.byref(tune)),
+               "gqf_batch_create")
+        self._h = h
+
+    def run(self, use_graph=True, stream=None) -> float:
+        ms = C.c_float(0.0)
+        _check(_lib().gqf_batch_run(self._h, int(bool(use_graph)), _stream_ptr(stream), C.byref(ms)),
+               "gqf_batch_run")
+        return ms.value
+
+    def tuning(self):
+        t = gqf_batch_tuning()
+        _check(_lib().gqf_batch_tuning_of(self._h, C.byref(t)), "gqf_batch_tuning_of")
+        return {"bucket_bits": t.bucket_bits, "scatter_chunk": t.scatter_chunk}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().gqf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -97,8 +97,8 @@ __device__ uint32_t block_exclusive_scan_u32(uint32_t *cnt, uint32_t nvals, uint
 // pair payload is the key's position in the input (sorted lookups).
 // ---------------------------------------------------------------------
 template <int THREADS, int IPT, bool PAIRS>
-__global__ void __launch_bounds__(THREADS) k_hash_bucket(
-    const uint32_t *__restrict__ keys, uint32_t n, BucketGeom g,
+__device__ __forceinline__ void hash_bucket_chunk(
+    uint32_t chunk, const uint32_t *__restrict__ keys, uint32_t n, const BucketGeom &g,
     const uint32_t *__restrict__ bucket_base, uint32_t cap,
     uint32_t *__restrict__ bucket_cnt, uint32_t *__restrict__ out,
     uint32_t *__restrict__ out_idx, uint32_t *__restrict__ err)
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(THREADS) k_hash_bucket(
     uint32_t *s_gb = s_cur + g.nb;
     __shared__ uint32_t s_warp[33];
     const int tid = threadIdx.x;
-    const uint64_t c0 = (uint64_t)blockIdx.x * CHUNK;
+    const uint64_t c0 = (uint64_t)chunk * CHUNK;
     const uint32_t cnt = (uint32_t)min((uint64_t)CHUNK, (uint64_t)n - c0);
 
     for (uint32_t i = tid; i < g.nb; i += THREADS) s_cur[i] = 0;
@@ -167,15 +167,25 @@ __global__ void __launch_bounds__(THREADS) k_hash_bucket(
     }
 }
 
+template <int THREADS, int IPT, bool PAIRS>
+__global__ void __launch_bounds__(THREADS) k_hash_bucket(
+    const uint32_t *__restrict__ keys, uint32_t n, BucketGeom g,
+    const uint32_t *__restrict__ bucket_base, uint32_t cap,
+    uint32_t *__restrict__ bucket_cnt, uint32_t *__restrict__ out,
+    uint32_t *__restrict__ out_idx, uint32_t *__restrict__ err)
+{
+    hash_bucket_chunk<THREADS, IPT, PAIRS>(blockIdx.x, keys, n, g, bucket_base, cap, bucket_cnt, out, out_idx, err);
+}
+
 // Histogram-only pass for exact bucket bases (used when a speculative
 // bucket overflowed).
 template <int THREADS, int IPT>
-__global__ void __launch_bounds__(THREADS) k_bucket_hist(
-    const uint32_t *__restrict__ keys, uint32_t n, BucketGeom g, uint32_t *__restrict__ bucket_cnt)
+__device__ __forceinline__ void bucket_hist_chunk(uint32_t chunk, const uint32_t *__restrict__ keys, uint32_t n,
+                                                  const BucketGeom &g, uint32_t *__restrict__ bucket_cnt)
 {
     extern __shared__ __align__(16) uint32_t smem_hist[];
     constexpr uint32_t CHUNK = THREADS * IPT;
-    const uint64_t c0 = (uint64_t)blockIdx.x * CHUNK;
+    const uint64_t c0 = (uint64_t)chunk * CHUNK;
     const uint32_t cnt = (uint32_t)min((uint64_t)CHUNK, (uint64_t)n - c0);
     for (uint32_t i = threadIdx.x; i < g.nb; i += THREADS) smem_hist[i] = 0;
     __syncthreads();
@@ -193,6 +203,13 @@ __global__ void __launch_bounds__(THREADS) k_bucket_hist(
     __syncthreads();
     for (uint32_t b = threadIdx.x; b < g.nb; b += THREADS)
         if (smem_hist[b]) atomicAdd(bucket_cnt + b, smem_hist[b]);
+}
+
+template <int THREADS, int IPT>
+__global__ void __launch_bounds__(THREADS) k_bucket_hist(
+    const uint32_t *__restrict__ keys, uint32_t n, BucketGeom g, uint32_t *__restrict__ bucket_cnt)
+{
+    bucket_hist_chunk<THREADS, IPT>(blockIdx.x, keys, n, g, bucket_cnt);
 }
 
 // ---------------------------------------------------------------------
@@ -409,7 +426,7 @@ __device__ __forceinline__ void walk_groups(const uint32_t *s_cnt, const Rem *s_
 // ---------------------------------------------------------------------
 // THREADS threads own QPT consecutive quotients each (S = THREADS * QPT).
 template <int THREADS, int QPT_, int BPE>
-__global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_layout(LayoutArgs a)
+__device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const uint32_t b)
 {
     using Rem = typename std::conditional<BPE == 1, uint8_t, uint16_t>::type;
     extern __shared__ __align__(16) uint8_t smem_layout[];
@@ -423,18 +440,14 @@ __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_l
     const uint32_t BUF = S + SPILL_SLOTS;  // slots the tile buffer holds
 
     __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_b, s_cin, s_cout, s_nfix, s_fbase;
+    __shared__ uint32_t s_cin, s_cout, s_nfix, s_fbase;
     __shared__ LayoutFn s_wfn[THREADS / 32];
     __shared__ LayoutFn s_wexcl[THREADS / 32];
     __shared__ uint32_t s_fix[256];
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) {
-        s_b = atomicAdd(a.ticket, 1u);
-        s_nfix = 0;
-    }
+    if (tid == 0) s_nfix = 0;
     __syncthreads();
-    const uint32_t b = s_b;
     const uint32_t na = a.A.count(b), nbn = a.B.count(b);
     const uint32_t n = na + nbn;
     const size_t abase = na ? a.A.start(b) : 0, bbase = nbn ? a.B.start(b) : 0;
@@ -680,31 +693,37 @@ __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_l
     if (bitmap) {
         const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
         uint32_t c = texcl.apply(cin);
-        uint32_t occ = 0;  // bit j: quotient qb + j occupied (and in this tile)
+        // occupied quotients of this thread; those below lo (their slot was
+        // written by an earlier bucket) become fix-ups
+        uint32_t nz = 0;
 #pragma unroll
-        for (uint32_t j = 0; j < QPT; j++) {
-            uint32_t m = mreg[j];
-            if (m) {
-                const uint32_t xa = x0 + qb + j;
-                uint32_t pos = xa > c ? xa : c;
-                if (xa >= lo) occ |= 1u << (j & 31);
-                else add_fix(xa);
-                uint32_t e0 = pos != xa ? 1u : 0u;  // shifted
-                do {
-                    uint32_t v = (uint32_t)__ffs(m) - 1u;
-                    m &= m - 1u;
-                    if (pos < hi) put_elem(pos, (v << 3) | e0);
-                    e0 = 3u;  // later items: continuation + shifted
-                    pos++;
-                } while (m);
-                c = pos;
+        for (uint32_t j = 0; j < QPT; j++) nz |= (mreg[j] != 0u ? 1u : 0u) << j;
+        const uint32_t xb = x0 + qb;
+        const uint32_t nbelow = lo > xb ? min(lo - xb, 32u) : 0u;
+        const uint32_t bmask = nbelow >= 32u ? 0xFFFFFFFFu : ((1u << nbelow) - 1u);
+        for (uint32_t fx = nz & bmask; fx; fx &= fx - 1u) add_fix(xb + (uint32_t)__ffs(fx) - 1u);
+        const uint32_t occ = nz & ~bmask;
+        if (QPT >= 32) s_occ[qb >> 5] = occ;  // this thread owns the whole word
+        else if (occ) atomicOr(s_occ + (qb >> 5), occ << (qb & 31));
+        // the thread's items in slot order, one per iteration (a loop per
+        // quotient would make the warp wait for its fullest quotient at
+        // every step); the next quotient's set comes from shared memory
+        uint32_t m = 0, pos = 0, e0 = 0, nzr = nz;
+        for (uint32_t it = 0; it < fn.n; it++) {
+            if (!m) {
+                const uint32_t j = (uint32_t)__ffs(nzr) - 1u;
+                nzr &= nzr - 1u;
+                m = s_mask[mask_word(qb + j)];
+                const uint32_t xa = xb + j;
+                pos = xa > c ? xa : c;
+                e0 = pos != xa ? 1u : 0u;  // shifted
             }
-            if (QPT >= 32 && (j & 31) == 31) {
-                s_occ[(qb + j) >> 5] = occ;  // this thread owns the whole word
-                occ = 0;
-            }
+            const uint32_t v = (uint32_t)__ffs(m) - 1u;
+            m &= m - 1u;
+            if (pos < hi) put_elem(pos, (v << 3) | e0);
+            e0 = 3u;  // later items of the run: continuation + shifted
+            c = ++pos;
         }
-        if (QPT < 32 && occ) atomicOr(s_occ + (qb >> 5), occ << (qb & 31));  // shared word
     } else {
         const LayoutFn texcl = compose(s_wexcl[wid], wexcl);
         uint32_t c = texcl.apply(cin);
@@ -773,6 +792,17 @@ __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_l
         }
         for (size_t g = b_end + tid; g < ge; g += THREADS) a.table[g] = byte_out(g);
     }
+}
+
+// One CTA per bucket, taken in ticket order so every bucket's predecessors
+// are running or done when it looks back.
+template <int THREADS, int QPT_, int BPE>
+__global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_layout(LayoutArgs a)
+{
+    __shared__ uint32_t s_ticket;
+    if (threadIdx.x == 0) s_ticket = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    bucket_layout_body<THREADS, QPT_, BPE>(a, s_ticket);
 }
 
 template <int BPE>

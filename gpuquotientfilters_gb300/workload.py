@@ -50,3 +50,24 @@ def config2(seed: int = 2, q: int = 26, r: int = 5, n: int = 53687091, n_insert:
     ins = mt19937(seed, n_insert, skip=n)
     look = mixed_lookups(keys, n_lookup, seed, skip=n + n_insert)
     return dict(q=q, r=r, keys=keys, inserts=ins, lookups=look, deletes=keys[:n_delete].copy())
+
+
+def config4(seed: int = 4, nfilters: int = 256, q_lo: int = 12, q_hi: int = 22):
+    """Batched multi-filter workload: nfilters independent r=5 filters,
+    q uniform in [q_lo, q_hi], fill uniform in [0.5, 0.9]; filter i draws its
+    keys from MT19937 seeded seed*1000 + i (one substream per filter; its
+    next draws are the negative lookups); lookup batch size Pareto(1.5)
+    clipped to [2^8, 2^20], 50% positive.  Shapes from numpy PCG64(seed)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(nfilters):
+        q = int(rng.integers(q_lo, q_hi + 1))
+        fill = float(rng.uniform(0.5, 0.9))
+        n = int(round(fill * (1 << q)))
+        nl = int(np.clip((rng.pareto(1.5) + 1.0) * 256.0, 256, 1 << 20))
+        keys = mt19937(seed * 1000 + i, n + nl - nl // 2)
+        pos = keys[rng.integers(0, n, nl // 2)]
+        look = np.concatenate([pos, keys[n:]]).astype(np.uint32)
+        look = look[rng.permutation(nl)]
+        out.append(dict(q=q, r=5, fill=fill, keys=keys[:n].copy(), lookups=look))
+    return out

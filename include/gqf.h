@@ -157,6 +157,40 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
 int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
                              int32_t *d_out, void *stream, float *ms);
 
+/* ---------------- batched filters (no counterpart in the reference) ----- */
+/* Many independent standard filters built and queried together: one launch
+ * of each pipeline kernel covers every filter of the batch (work lists of
+ * scatter chunks, buckets and query chunks across all filters), and the
+ * launch sequence is captured once into a CUDA graph.  A job bulk builds
+ * its filter from n_build keys (as gqf_sqf_bulk_build; n_build == 0 leaves
+ * the table as it is), then answers n_lookup unsorted lookups (as
+ * gqf_sqf_lookup_unsorted).  All filters of a batch share r.  The batch
+ * keeps the job pointers: run it again after refilling the same buffers.
+ * Every filter that is rebuilt needs q >= the tuning's bucket bits. */
+typedef struct gqf_sqf_job {
+    gqf_sqf filter;
+    int n_build;
+    const uint32_t *d_build_keys;
+    int n_lookup;
+    const uint32_t *d_lookup_keys;
+    uint32_t *d_results;
+} gqf_sqf_job;
+/* Launch shape of a batch (0 = default): bucket_bits = log2 quotients per
+ * layout CTA (10..13, default 12); scatter_chunk = keys per scatter CTA
+ * (2048, 8192 or 32768, default 8192). */
+typedef struct gqf_batch_tuning {
+    int bucket_bits;
+    int scatter_chunk;
+} gqf_batch_tuning;
+typedef struct gqf_batch gqf_batch;
+int gqf_batch_create(gqf_batch **out, const gqf_sqf_job *jobs, int count, int no_duplicates,
+                     const gqf_batch_tuning *tuning);
+/* use_graph != 0: one cudaGraphLaunch of the captured pipeline; 0: the same
+ * kernels launched directly on `stream` */
+int gqf_batch_run(gqf_batch *batch, int use_graph, void *stream, float *ms);
+int gqf_batch_tuning_of(const gqf_batch *batch, gqf_batch_tuning *out);
+int gqf_batch_destroy(gqf_batch *batch);
+
 /* ---------------- serialization (no counterpart in the reference) ------- */
 /* Checkpoint / restore of a filter as one host image: a 64-byte header
  * (magic "GQFSQF01" or "GQFRSQF1", format version, q, r, payload bytes,
