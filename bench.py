@@ -215,10 +215,11 @@ def run_gpu(args, world, rank, local):
     del d_keys, d_look, d_ins, d_del, d_out, d_out2
     rsqf = rsqf_ops(args, G, torch, dev, stream, flush, peak) if args.rsqf and not wanted else None
     batched = batched_ops(args, G, torch, dev, stream, flush, peak) if args.batched and not wanted else None
+    served = served_ops(args, G, torch, dev) if args.served and not wanted else None
     return {
         "value": value, "ms_per_step": t_max / args.steps, "per_op": per_op, "clocks": clk,
         "gpu_launches": int(launches), "peak": peak, "peak_kind": peak_kind, "e2e": e2e, "rsqf": rsqf,
-        "batched": batched,
+        "batched": batched, "served": served,
         "roofline": {"bound": "hbm", "kernel": "bulk build pipeline (hash+bucket scatter, bucket layout, fixup)",
                      "achieved": b["alg_GBps"], "peak": peak, "unit": "GB/s", "frac": b["frac_hbm"],
                      "traffic": None, "peak_source": peak_kind},
@@ -347,6 +348,108 @@ def batched_ops(args, G, torch, dev, stream, flush, peak):
             "results_identical": bool(same)}
 
 
+def served_ops(args, G, torch, dev):
+    """Served stream (64 resident r=5 filters, q in [16,24], fill 0.6; 400
+    requests of log-uniform size in [2^8, 2^20], 70% lookups / 20% inserts /
+    10% deletes, Zipf(1.1) keys over 2^30, deletes of present keys): the
+    continuous-batching server against the plain path (each request in turn:
+    copy keys in, one synchronous API call, copy results out), both from
+    pinned host buffers, wall-clock timed.  Saturation: all requests offered
+    at once.  Latency: Poisson arrivals at fractions of the saturation rate
+    (filters rebuilt before each run).  Results and final tables of the
+    saturation run are compared with the plain path's."""
+    import time as _t
+    from gpuquotientfilters_gb300 import workload as W
+    filters, reqs = W.config5()
+    budget = 8 << 30
+
+    def build_all():
+        qfs = [G.initFilterGPU(f["q"], 5) for f in filters]
+        keys = [torch.from_numpy(f["keys"].view(np.int32)).to(dev) for f in filters]
+        b = G.Batch([(qf, k, None, None) for qf, k in zip(qfs, keys)], True)
+        b.run()
+        b.close()
+        torch.cuda.synchronize(dev)
+        return qfs
+
+    h_keys = [torch.from_numpy(r["keys"].view(np.int32)).pin_memory() for r in reqs]
+    nkeys = sum(r["keys"].size for r in reqs)
+
+    def new_outs():
+        return [torch.zeros(max(r["keys"].size, 1), dtype=torch.int32).pin_memory() if r["op"] == 0 else None
+                for r in reqs]
+
+    def run_served(qfs, outs, arrivals=None):
+        srv = G.Server(qfs, hbm_budget=budget)
+        info = srv.info()
+        t0 = _t.perf_counter()
+        for i, (r, k, o) in enumerate(zip(reqs, h_keys, outs)):
+            if arrivals is not None:
+                while _t.perf_counter() - t0 < arrivals[i]:
+                    pass
+            srv.submit(r["filter"], r["op"], k, o)
+        srv.drain()
+        wall = _t.perf_counter() - t0
+        done = srv.poll(len(reqs) + 16)
+        srv.close()
+        lat = np.array([d["done_us"] - d["submit_us"] for d in done])
+        return wall, lat, info, all(d["status"] == 0 for d in done)
+
+    # saturation
+    served_q = build_all()
+    outs_s = new_outs()
+    wall_s, lat_s, info, ok_s = run_served(served_q, outs_s)
+    # plain path on a second copy
+    plain_q = build_all()
+    outs_p = new_outs()
+    d_keys = torch.empty(max(r["keys"].size for r in reqs), dtype=torch.int32, device=dev)
+    d_out = torch.empty_like(d_keys)
+    lat_p = []
+    t0 = _t.perf_counter()
+    for r, k, o in zip(reqs, h_keys, outs_p):
+        ts = _t.perf_counter()
+        n = r["keys"].size
+        d_keys[:n].copy_(k)
+        qf = plain_q[r["filter"]]
+        if r["op"] == 0:
+            G.launchUnsortedLookups(qf, n, d_keys, d_out)
+            o[:n].copy_(d_out[:n])
+        elif r["op"] == 1:
+            G.insert(qf, n, d_keys)
+        else:
+            G.superclusterDeletes(qf, n, d_keys)
+        lat_p.append((_t.perf_counter() - t0) * 1e6)  # all offered at t0: completion time = latency
+    wall_p = _t.perf_counter() - t0
+    same = all(torch.equal(a, b) for a, b in zip(outs_s, outs_p) if a is not None) and all(
+        np.array_equal(G.table_bytes(a), G.table_bytes(b)) for a, b in zip(served_q, plain_q))
+    for qf in served_q + plain_q:
+        G.freeFilterGPU(qf)
+    sat_rps = len(reqs) / wall_s
+    sweep = []
+    rng = np.random.Generator(np.random.PCG64(55))
+    for frac in (0.25, 0.5, 0.75):
+        rate = frac * sat_rps
+        arr = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+        qfs = build_all()
+        wall, lat, _, ok = run_served(qfs, new_outs(), arr)
+        for qf in qfs:
+            G.freeFilterGPU(qf)
+        sweep.append({"offered_req_per_s": round(rate, 1), "achieved_Mkeys_per_s": round(nkeys / wall / 1e6, 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)) / 1e3, 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)) / 1e3, 3), "ok": bool(ok)})
+    return {"workload": "64 SQFs r=5 q U[16,24] fill 0.6; 400 requests log-uniform [2^8,2^20] keys, 70/20/10 "
+                        "lookup/insert/delete, Zipf(1.1) over 2^30, seed 5; HBM budget 8 GiB",
+            "requests": len(reqs), "keys": int(nkeys), "streams": info["streams"],
+            "hbm_bytes": info["hbm_bytes"],
+            "served_Mkeys_per_s": round(nkeys / wall_s / 1e6, 1), "plain_Mkeys_per_s": round(nkeys / wall_p / 1e6, 1),
+            "throughput_ratio": round(wall_p / wall_s, 2),
+            "saturation_p50_ms": round(float(np.percentile(lat_s, 50)) / 1e3, 3),
+            "saturation_p99_ms": round(float(np.percentile(lat_s, 99)) / 1e3, 3),
+            "plain_p50_ms": round(float(np.percentile(lat_p, 50)) / 1e3, 3),
+            "plain_p99_ms": round(float(np.percentile(lat_p, 99)) / 1e3, 3),
+            "poisson_sweep": sweep, "results_identical": bool(same and ok_s)}
+
+
 def e2e_step(args, G, torch, dev, stream, c, qf):
     """The same step from pinned host memory: copies in, ops, results out."""
     def pinned(a):
@@ -462,6 +565,7 @@ def main():
                     "values scale every batch by 2^(q-26), for profiling small cases)")
     ap.add_argument("--no-rsqf", dest="rsqf", action="store_false", help="skip the RSQF ops")
     ap.add_argument("--no-batched", dest="batched", action="store_false", help="skip the batched-filter ops")
+    ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served-stream ops")
     ap.add_argument("--ops", default="", help="comma list of ops to run (build always runs)")
     args = ap.parse_args()
     world, rank, local = dist_init()
@@ -487,6 +591,7 @@ def main():
                    "parallelism": "replicas x%d" % world},
         "per_op": r["per_op"], "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"],
         "clocks": r["clocks"], "gpu_launches": r["gpu_launches"], "rsqf": r["rsqf"], "batched": r["batched"],
+        "served": r["served"],
     }
     print(json.dumps(out), flush=True)
 

@@ -49,6 +49,16 @@ class gqf_batch_tuning(C.Structure):
     _fields_ = [("bucket_bits", C.c_int), ("scatter_chunk", C.c_int)]
 
 
+class gqf_server_config(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_streams", C.c_int), ("max_op_keys", C.c_int),
+                ("coalesce", C.c_int)]
+
+
+class gqf_completion(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int), ("submit_us", C.c_double), ("start_us", C.c_double),
+                ("done_us", C.c_double)]
+
+
 class countingQuotientFilterGPU(C.Structure):
     """struct countingQuotientFilterGPU (RSQF.cuh:32-37)."""
     _fields_ = [("qbits", C.c_uint), ("numBlocks", C.c_uint), ("blocks", C.c_void_p)]
@@ -101,6 +111,15 @@ def _lib():
             "gqf_batch_run": (i32, [C.c_void_p, i32, vp, f32p]),
             "gqf_batch_tuning_of": (i32, [C.c_void_p, C.POINTER(gqf_batch_tuning)]),
             "gqf_batch_destroy": (i32, [C.c_void_p]),
+            "gqf_workspace_reserve": (i32, [vp, C.c_size_t, C.POINTER(C.c_size_t)]),
+            "gqf_workspace_release": (i32, [vp]),
+            "gqf_sqf_update_workspace_bytes": (C.c_size_t, [C.c_uint, C.c_uint, i32]),
+            "gqf_server_create": (i32, [C.POINTER(C.c_void_p), qfp, i32, C.POINTER(gqf_server_config)]),
+            "gqf_server_submit": (i32, [C.c_void_p, i32, i32, vp, i32, vp, C.POINTER(C.c_uint64)]),
+            "gqf_server_poll": (i32, [C.c_void_p, C.POINTER(gqf_completion), i32, C.POINTER(C.c_int)]),
+            "gqf_server_drain": (i32, [C.c_void_p]),
+            "gqf_server_info": (i32, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
+            "gqf_server_destroy": (i32, [C.c_void_p]),
             "gqf_sqf_image_bytes": (C.c_size_t, [qfp]),
             "gqf_rsqf_image_bytes": (C.c_size_t, [cqfp]),
             "gqf_sqf_save": (i32, [qfp, vp, C.c_size_t, vp]),
@@ -417,6 +436,73 @@ class Batch:
         if getattr(self, "_h", None):
             _lib().gqf_batch_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------- served filters
+SERVE_LOOKUP, SERVE_INSERT, SERVE_DELETE = 0, 1, 2
+
+
+class Server:
+    """Request loop with continuous batching over resident filters
+    (gqf_server_* in include/gqf.h).  submit() takes host buffers (pinned
+    torch tensors or numpy arrays) and keeps them alive until the request
+    completes; results of a lookup land in its results buffer."""
+
+    def __init__(self, filters, hbm_budget=0, max_streams=0, max_op_keys=0, coalesce=True):
+        arr = (quotient_filter * len(filters))(*filters)
+        cfg = gqf_server_config(int(hbm_budget), int(max_streams), int(max_op_keys), int(bool(coalesce)))
+        h = C.c_void_p()
+        _check(_lib().gqf_server_create(C.byref(h), arr, len(filters), C.byref(cfg)), "gqf_server_create")
+        self._h = h
+        self._live = {}
+
+    @staticmethod
+    def _host_ptr(x):
+        if x is None:
+            return 0
+        if hasattr(x, "data_ptr"):
+            return int(x.data_ptr())
+        return int(x.ctypes.data)
+
+    def submit(self, filt: int, op: int, keys, results=None) -> int:
+        rid = C.c_uint64()
+        n = int(keys.numel() if hasattr(keys, "numel") else keys.size)
+        _check(_lib().gqf_server_submit(self._h, int(filt), int(op), self._host_ptr(keys), n,
+                                        self._host_ptr(results), C.byref(rid)), "gqf_server_submit")
+        self._live[rid.value] = (keys, results)
+        return rid.value
+
+    def poll(self, max_items=4096):
+        buf = (gqf_completion * max_items)()
+        cnt = C.c_int()
+        _check(_lib().gqf_server_poll(self._h, buf, max_items, C.byref(cnt)), "gqf_server_poll")
+        out = []
+        for i in range(cnt.value):
+            c = buf[i]
+            self._live.pop(c.id, None)
+            out.append({"id": c.id, "status": c.status, "submit_us": c.submit_us, "start_us": c.start_us,
+                        "done_us": c.done_us})
+        return out
+
+    def drain(self):
+        _check(_lib().gqf_server_drain(self._h), "gqf_server_drain")
+
+    def info(self):
+        ns, hb = C.c_int(), C.c_size_t()
+        _check(_lib().gqf_server_info(self._h, C.byref(ns), C.byref(hb)), "gqf_server_info")
+        return {"streams": ns.value, "hbm_bytes": hb.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().gqf_server_destroy(self._h)
+            self._h = None
+            self._live.clear()
 
     def __del__(self):
         try:

@@ -4,6 +4,8 @@
 
 #include <atomic>
 #include <cstring>
+#include <map>
+#include <memory>
 
 namespace gqf {
 
@@ -39,10 +41,37 @@ const DeviceInfo &device_info(int dev)
     return d;
 }
 
-Arena &arena(int dev)
+// One arena per (device, stream): calls on one stream run in order and
+// reuse its scratch; calls on different streams get different scratch, so
+// they may overlap on the device.
+static std::mutex g_arena_mu;
+static std::map<std::pair<int, cudaStream_t>, std::unique_ptr<Arena>> g_arenas;
+
+Arena &arena(int dev, cudaStream_t s)
 {
-    static Arena arenas[64];
-    return arenas[dev & 63];
+    std::lock_guard<std::mutex> lk(g_arena_mu);
+    std::unique_ptr<Arena> &a = g_arenas[std::make_pair(dev, s)];
+    if (!a) a.reset(new Arena());
+    return *a;
+}
+
+int release_arena(int dev, cudaStream_t s)
+{
+    std::unique_ptr<Arena> a;
+    {
+        std::lock_guard<std::mutex> lk(g_arena_mu);
+        auto it = g_arenas.find(std::make_pair(dev, s));
+        if (it == g_arenas.end()) return GQF_OK;
+        std::lock_guard<std::mutex> lk2(it->second->mu);
+        a = std::move(it->second);
+        g_arenas.erase(it);
+    }
+    GQF_CK(cudaStreamSynchronize(s));
+    if (a->ptr) GQF_CK(cudaFree(a->ptr));
+    if (a->latch) GQF_CK(cudaFree(a->latch));
+    if (a->ev0) cudaEventDestroy(a->ev0);
+    if (a->ev1) cudaEventDestroy(a->ev1);
+    return GQF_OK;
 }
 
 void *arena_reserve(Arena &a, size_t bytes)
@@ -137,10 +166,10 @@ const char *gqf_status_string(int st)
 int gqf_stream_status(void *stream)
 {
     int dev = current_device();
-    Arena &a = arena(dev);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Arena &a = arena(dev, s);
     std::lock_guard<std::mutex> lk(a.mu);
     if (!arena_reserve(a, 0)) return GQF_ERR_NOMEM;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     GQF_CK(cudaStreamSynchronize(s));
     uint32_t e = 0;
     GQF_CK(cudaMemcpy(&e, a.latch, sizeof(e), cudaMemcpyDeviceToHost));
@@ -149,6 +178,18 @@ int gqf_stream_status(void *stream)
 }
 
 unsigned long long gqf_kernel_launches(void) { return g_launches.load(); }
+
+int gqf_workspace_reserve(void *stream, size_t bytes, size_t *reserved)
+{
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Arena &a = arena(current_device(), s);
+    std::lock_guard<std::mutex> lk(a.mu);
+    if (!arena_reserve(a, bytes)) return GQF_ERR_NOMEM;
+    if (reserved) *reserved = a.size;
+    return GQF_OK;
+}
+
+int gqf_workspace_release(void *stream) { return release_arena(current_device(), static_cast<cudaStream_t>(stream)); }
 
 unsigned int gqf_aphash(unsigned int value, unsigned int table_size)
 {

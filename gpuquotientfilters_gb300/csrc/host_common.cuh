@@ -30,8 +30,9 @@ struct DeviceInfo {
 };
 const DeviceInfo &device_info(int dev);
 
-// Grow-only scratch arena, one per device.  Calls on one device are
-// serialised by the arena mutex held for the duration of each entry point.
+// Grow-only scratch arena, one per (device, stream).  Calls on one stream
+// are serialised by the arena mutex held for the duration of each entry
+// point and run in stream order on the device.
 struct Arena {
     void *ptr = nullptr;
     size_t size = 0;
@@ -40,7 +41,9 @@ struct Arena {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
 };
-Arena &arena(int dev);
+Arena &arena(int dev, cudaStream_t s);
+// Frees the arena of (dev, s) after the stream drains.
+int release_arena(int dev, cudaStream_t s);
 // Ensures the arena holds `bytes`; returns its base (nullptr on failure).
 void *arena_reserve(Arena &a, size_t bytes);
 

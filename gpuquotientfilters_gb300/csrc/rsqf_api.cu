@@ -306,7 +306,7 @@ int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
 {
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    Arena &ar = arena(current_device());
+    Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
     int st = call_begin(ar, s, ms != nullptr);
     if (st) return st;
@@ -355,7 +355,7 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, i
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const BucketGeom g = rsqf_geom(cqf->qbits, (uint64_t)n);
-    Arena &ar = arena(current_device());
+    Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
     Sizer z;
     z.take<uint32_t>(g.nb);
@@ -423,7 +423,7 @@ int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t 
     const size_t tbytes = rsqf_table_bytes(nbl);
     const uint32_t ntiles = (nbl + 1 + PEND_TILE - 1) / PEND_TILE;
     uint8_t *table = static_cast<uint8_t *>(cqf->blocks);
-    Arena &ar = arena(current_device());
+    Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
     Sizer z;
     z.take<uint32_t>(g.nb);

@@ -293,6 +293,21 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
 
 enum class Src { NONE, TABLE, KEYS, TABLE2 };
 
+// Scratch bytes of rebuild() for an insert or delete of n keys (the same
+// sizing as below).
+static size_t update_scratch_bytes(uint32_t q, uint32_t r, uint32_t n)
+{
+    const uint32_t nslots = gqf_sqf_num_slots(q);
+    const uint64_t expect = std::min<uint64_t>((uint64_t)(nslots * 0.9) + n, (uint64_t)nslots * 2);
+    LayoutPlan p = plan_layout(q, r, expect, n, r == 5);
+    ScratchReq req{p.g.nb, (size_t)p.g.nb * p.stride, false, true, false, nslots};
+    size_t bytes = 0, bytes_exact = 0;
+    carve(nullptr, req, true, &bytes);
+    req.batch_items = std::max<size_t>(n, 1);
+    carve(nullptr, req, true, &bytes_exact);
+    return std::max(bytes, bytes_exact);
+}
+
 // One rebuild: A = current contents of `table` (when the op needs them) or
 // of `table2`, B = hashed batch keys (or the second table's contents).
 template <int BPE>
@@ -315,7 +330,7 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
     (void)nA;
     (void)nB;
     int dev = current_device();
-    Arena &ar = arena(dev);
+    Arena &ar = arena(dev, s);
     std::lock_guard<std::mutex> lk(ar.mu);
     size_t bytes = 0;
     carve(nullptr, req, true, &bytes);
@@ -377,7 +392,7 @@ template <int BPE>
 static int lookup_unsorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint32_t *out, cudaStream_t s, float *ms)
 {
     const SqfGeom tg = geom_of(qf);
-    Arena &ar = arena(current_device());
+    Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
     int st = call_begin(ar, s, ms != nullptr);
     if (st) return st;
@@ -399,7 +414,7 @@ static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint3
     LayoutPlan p = plan_layout(tg.q, tg.r, (uint64_t)tg.nslots * 8 / 10, (uint64_t)n, false);
     // query buckets: aim for ~4k queries per bucket, table-aligned
     ScratchReq req{p.g.nb, (size_t)std::max(n, 1), true, false, false, tg.nslots};
-    Arena &ar = arena(current_device());
+    Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
     size_t bytes = 0;
     carve(nullptr, req, true, &bytes);
@@ -485,6 +500,12 @@ size_t gqf_sqf_table_bytes(unsigned int q, unsigned int r)
 }
 
 unsigned int gqf_sqf_num_slots(unsigned int q) { return (unsigned int)((double)(1u << q) * 1.1); }
+
+size_t gqf_sqf_update_workspace_bytes(unsigned int q, unsigned int r, int n)
+{
+    if (!qr_ok(q, r) || n < 0) return 0;
+    return align_up(update_scratch_bytes(q, r, (uint32_t)n), 1u << 20);
+}
 
 int gqf_sqf_init(gqf_sqf *qf, unsigned int q, unsigned int r)
 {

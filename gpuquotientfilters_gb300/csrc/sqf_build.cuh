@@ -131,13 +131,23 @@ __device__ __forceinline__ void hash_bucket_chunk(
         if (j < cnt) atomicAdd(&s_cur[fp[k] >> g.shift], 1u);
     }
     __syncthreads();
-    // exclusive offsets + one global reservation per non-empty bucket
+    // one global reservation per non-empty bucket; a thread's reservations
+    // (buckets tid, tid + THREADS, ...) are issued together so their round
+    // trips overlap
     {
-        const uint32_t per = (g.nb + THREADS - 1) / THREADS;
-        const uint32_t beg = min(g.nb, tid * per), end = min(g.nb, beg + per);
-        for (uint32_t b = beg; b < end; b++) {
-            uint32_t c = s_cur[b];
-            s_gb[b] = c ? atomicAdd(bucket_cnt + b, c) : 0u;
+        constexpr uint32_t MAXPER = (4096 + THREADS - 1) / THREADS;  // nb <= 4096
+        uint32_t c[MAXPER], r[MAXPER];
+#pragma unroll
+        for (uint32_t k = 0; k < MAXPER; k++) {
+            const uint32_t b = tid + k * THREADS;
+            c[k] = b < g.nb ? s_cur[b] : 0u;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < MAXPER; k++) r[k] = c[k] ? atomicAdd(bucket_cnt + tid + k * THREADS, c[k]) : 0u;
+#pragma unroll
+        for (uint32_t k = 0; k < MAXPER; k++) {
+            const uint32_t b = tid + k * THREADS;
+            if (b < g.nb) s_gb[b] = r[k];
         }
     }
     block_exclusive_scan_u32<THREADS>(s_cur, g.nb, s_warp);

@@ -71,3 +71,51 @@ def config4(seed: int = 4, nfilters: int = 256, q_lo: int = 12, q_hi: int = 22):
         look = look[rng.permutation(nl)]
         out.append(dict(q=q, r=5, fill=fill, keys=keys[:n].copy(), lookups=look))
     return out
+
+
+def zipf_keys(rng, n: int, s: float = 1.1, universe_bits: int = 30) -> np.ndarray:
+    """n keys from a Zipf(s) law over a 2^universe_bits universe: rank v
+    (numpy's zipf sampler, v >= 1) is scrambled by an odd multiplier mod
+    2^32 and kept to universe_bits bits, so hot keys are spread over the
+    key space."""
+    v = rng.zipf(s, n).astype(np.uint64)
+    return (((v * np.uint64(0x9E3779B1)) & np.uint64(0xFFFFFFFF)) >> np.uint64(32 - universe_bits)).astype(np.uint32)
+
+
+def config5(seed: int = 5, nfilters: int = 64, q_lo: int = 16, q_hi: int = 24, fill: float = 0.6,
+            nreq: int = 400, size_lo: int = 1 << 8, size_hi: int = 1 << 20, mix=(0.7, 0.2, 0.1)):
+    """Served stream: nfilters resident r=5 filters (q uniform in
+    [q_lo, q_hi]), each bulk built to `fill` from MT19937 seed*1000+i keys;
+    nreq requests, each on a uniformly chosen filter, kind drawn by `mix`
+    (lookup, insert, delete), size log-uniform in [size_lo, size_hi].
+    Lookup and insert keys are Zipf(1.1) over a 2^30 universe; delete keys
+    are present keys (the filter's initial keys, each deleted at most once).
+    An insert batch is capped at 2^(q-4) keys of its filter (1/16 of the
+    slots), so the smallest filters do not overflow their 1.1 * 2^q slots.
+    Shapes and draws from numpy PCG64(seed)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    filters = []
+    order, cursor = [], []
+    for i in range(nfilters):
+        q = int(rng.integers(q_lo, q_hi + 1))
+        keys = mt19937(seed * 1000 + i, int(round(fill * (1 << q))))
+        filters.append(dict(q=q, r=5, keys=keys))
+        order.append(rng.permutation(keys.size))
+        cursor.append(0)
+    reqs = []
+    kinds = rng.choice(3, size=nreq, p=np.asarray(mix, float) / sum(mix))
+    for k in kinds:
+        f = int(rng.integers(0, nfilters))
+        n = int(np.exp(rng.uniform(np.log(size_lo), np.log(size_hi + 1))))
+        n = min(max(n, size_lo), size_hi)
+        if k == 1:
+            n = min(n, 1 << (filters[f]["q"] - 4))
+        if k == 2:
+            c = cursor[f]
+            n = min(n, filters[f]["keys"].size - c)
+            keys = filters[f]["keys"][order[f][c:c + n]]
+            cursor[f] = c + n
+        else:
+            keys = zipf_keys(rng, n)
+        reqs.append(dict(filter=f, op=int(k), keys=np.ascontiguousarray(keys, np.uint32)))
+    return filters, reqs

@@ -79,6 +79,15 @@ const char *gqf_status_string(int status);
 unsigned long long gqf_kernel_launches(void);
 /* latched device error for `stream` since the last call (waits for it) */
 int gqf_stream_status(void *stream);
+/* Scratch workspaces (no reference counterpart): every stream has its own,
+ * grown on demand and kept, so calls on different streams may overlap on
+ * the device.  reserve pre-grows a stream's workspace (a later call that
+ * fits allocates nothing); release frees it after the stream drains. */
+int gqf_workspace_reserve(void *stream, size_t bytes, size_t *reserved);
+int gqf_workspace_release(void *stream);
+/* Workspace bytes one gqf_sqf_insert / gqf_sqf_delete of n keys on a
+ * filter of (q, r) needs. */
+size_t gqf_sqf_update_workspace_bytes(unsigned int q, unsigned int r, int n);
 
 /* ---------------- standard quotient filter ------------------------------ */
 /* initFilterGPU, quotientFilter.cu:44-55.  Allocates and ZEROES the table
@@ -190,6 +199,42 @@ int gqf_batch_create(gqf_batch **out, const gqf_sqf_job *jobs, int count, int no
 int gqf_batch_run(gqf_batch *batch, int use_graph, void *stream, float *ms);
 int gqf_batch_tuning_of(const gqf_batch *batch, gqf_batch_tuning *out);
 int gqf_batch_destroy(gqf_batch *batch);
+
+/* ---------------- served filters (no counterpart in the reference) ------ */
+/* A request loop over resident filters with continuous batching: requests
+ * (a lookup, insert or delete batch on one filter, host key buffers) are
+ * queued per filter; whenever a device stream slot frees up, the filter
+ * whose oldest request waited longest gets an op made of all its queued
+ * requests of that request's kind (consecutive same-kind requests coalesce;
+ * the result is the one of applying them one by one).  Ops of different
+ * filters run concurrently on separate streams, one op per filter at a
+ * time, so every filter sees its requests in submission order.  The HBM
+ * budget bounds tables + per-stream workspaces + staging: it fixes how many
+ * streams (ops in flight) the server runs.  Key and result buffers must
+ * stay valid until the request completes (pinned memory lets copies
+ * overlap). */
+enum { GQF_SERVE_LOOKUP = 0, GQF_SERVE_INSERT = 1, GQF_SERVE_DELETE = 2 };
+typedef struct gqf_server_config {
+    size_t hbm_budget_bytes; /* 0: no limit beyond the device's memory     */
+    int max_streams;         /* concurrent ops at most (0: 8)              */
+    int max_op_keys;         /* keys per coalesced op (0: 2^22)            */
+    int coalesce;            /* 0: one request per op                      */
+} gqf_server_config;
+typedef struct gqf_completion {
+    uint64_t id;
+    int status;
+    double submit_us, start_us, done_us; /* since the server started      */
+} gqf_completion;
+typedef struct gqf_server gqf_server;
+int gqf_server_create(gqf_server **out, const gqf_sqf *filters, int nfilters, const gqf_server_config *cfg);
+int gqf_server_submit(gqf_server *srv, int filter, int op, const uint32_t *keys, int n, uint32_t *results,
+                      uint64_t *id);
+/* completed requests since the last poll (at most max) */
+int gqf_server_poll(gqf_server *srv, gqf_completion *out, int max, int *count);
+/* waits until every submitted request has completed */
+int gqf_server_drain(gqf_server *srv);
+int gqf_server_info(const gqf_server *srv, int *streams, size_t *hbm_bytes);
+int gqf_server_destroy(gqf_server *srv);
 
 /* ---------------- serialization (no counterpart in the reference) ------- */
 /* Checkpoint / restore of a filter as one host image: a 64-byte header
