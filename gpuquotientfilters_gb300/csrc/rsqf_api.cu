@@ -147,13 +147,16 @@ __global__ void __launch_bounds__(SORT_THREADS) k_bucket_sort(uint32_t *items, c
     }
 }
 
-// Lists this round's groups: every active group start with batch items;
-// groups of at most RSQF_WARP_GROUP_MAX blocks go to the warp list, larger
-// ones to the list replayed by one thread each.
-constexpr uint32_t RSQF_WARP_GROUP_MAX = 224;  // blocks one warp stages (14 KB)
+// Lists this round's groups: every active group start with batch items.
+// Groups of at most RSQF_SMALL_GROUP blocks (nearly all of an incremental
+// batch) go to list 0, replayed by warps with small staging areas, many per
+// SM; groups of at most RSQF_WARP_GROUP_MAX blocks to list 1; larger ones to
+// list 2, replayed by one thread each in global memory.
+constexpr uint32_t RSQF_SMALL_GROUP = 16;      // 1 KB of staging per warp
+constexpr uint32_t RSQF_WARP_GROUP_MAX = 224;  // 14 KB of staging per warp
 __global__ void k_rsqf_groups(uint32_t nblocks, const uint8_t *__restrict__ start, uint8_t *__restrict__ active,
-                              const uint32_t *__restrict__ fhome, uint32_t *__restrict__ wlist,
-                              uint32_t *__restrict__ blist, uint32_t *__restrict__ counts)
+                              const uint32_t *__restrict__ fhome, uint32_t *__restrict__ list0,
+                              uint32_t *__restrict__ list1, uint32_t *__restrict__ list2, uint32_t *__restrict__ counts)
 {
     const uint32_t total = nblocks + 1;  // logical blocks + guard block
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < total; b += gridDim.x * blockDim.x) {
@@ -162,35 +165,32 @@ __global__ void k_rsqf_groups(uint32_t nblocks, const uint8_t *__restrict__ star
         uint32_t e = b + 1;
         while (e < total && !start[e]) e++;
         if (fhome[min(b, nblocks)] == fhome[min(e, nblocks)]) continue;  // no items: table unchanged
-        if (e - b <= RSQF_WARP_GROUP_MAX) {
-            const uint32_t k = atomicAdd(counts, 1u);
-            wlist[2 * k] = b;
-            wlist[2 * k + 1] = e;
-        } else {
-            const uint32_t k = atomicAdd(counts + 1, 1u);
-            blist[2 * k] = b;
-            blist[2 * k + 1] = e;
-        }
+        const int which = e - b <= RSQF_SMALL_GROUP ? 0 : (e - b <= RSQF_WARP_GROUP_MAX ? 1 : 2);
+        uint32_t *list = which == 0 ? list0 : (which == 1 ? list1 : list2);
+        const uint32_t k = atomicAdd(counts + which, 1u);
+        list[2 * k] = b;
+        list[2 * k + 1] = e;
     }
 }
 
-// One replay round, a warp per listed group: stage the group's blocks from
-// t0, insert its items (fhome: first sorted index homed at or past each
-// block) in ascending order, write the blocks back unless a write left the
-// group (then the group is marked crossed and t is left as it was).
-__global__ void __launch_bounds__(32) k_rsqf_round_warp(uint8_t *__restrict__ t, const uint8_t *__restrict__ t0,
-                                                        uint32_t nblocks, uint32_t q, const uint32_t *__restrict__ fps,
-                                                        const uint32_t *__restrict__ fhome,
-                                                        const uint32_t *__restrict__ wlist,
-                                                        const uint32_t *__restrict__ counts,
-                                                        uint8_t *__restrict__ crossed, uint32_t *n_crossed,
-                                                        int32_t *__restrict__ ret, int t0_zero)
+// One replay round, a warp per listed group (WARPS warps per CTA, each with
+// its own MAXB-block staging area): stage the group's blocks from t0,
+// insert its items (fhome: first sorted index homed at or past each block)
+// in ascending order, write the blocks back unless a write left the group
+// (then the group is marked crossed and t is left as it was).
+template <uint32_t MAXB, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_rsqf_round_warp(
+    uint8_t *__restrict__ t, const uint8_t *__restrict__ t0, uint32_t nblocks, uint32_t q,
+    const uint32_t *__restrict__ fps, const uint32_t *__restrict__ fhome, const uint32_t *__restrict__ list,
+    const uint32_t *__restrict__ count, uint8_t *__restrict__ crossed, uint32_t *n_crossed,
+    int32_t *__restrict__ ret, int t0_zero)
 {
-    __shared__ __align__(16) uint8_t sm[RSQF_WARP_GROUP_MAX * RSQF_SB];
-    const uint32_t lane = threadIdx.x;
-    const uint32_t ng = counts[0];
-    for (uint32_t gi = blockIdx.x; gi < ng; gi += gridDim.x) {
-        const uint32_t b = wlist[2 * gi], e = wlist[2 * gi + 1];
+    __shared__ __align__(16) uint8_t sm_all[WARPS][MAXB * RSQF_SB];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint8_t *sm = sm_all[wid];
+    const uint32_t ng = *count;
+    for (uint32_t gi = blockIdx.x * WARPS + wid; gi < ng; gi += gridDim.x * WARPS) {
+        const uint32_t b = list[2 * gi], e = list[2 * gi + 1];
         for (uint32_t i = lane; i < (e - b) * 8; i += 32) {
             const uint32_t blk = b + i / 8, w = i % 8;
             const uint8_t *src = t0 + (size_t)blk * RSQF_BB;
@@ -232,7 +232,7 @@ __global__ void k_rsqf_round_big(uint8_t *t, const uint8_t *t0, uint32_t nblocks
                                  const uint32_t *fhome, const uint32_t *blist, const uint32_t *counts,
                                  uint8_t *crossed, uint32_t *n_crossed, int32_t *ret, int t0_zero)
 {
-    const uint32_t ng = counts[1];
+    const uint32_t ng = counts[2];
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ng; gi += gridDim.x * blockDim.x) {
         const uint32_t b = blist[2 * gi], e = blist[2 * gi + 1];
         for (size_t i = (size_t)b * RSQF_BB; i < (size_t)e * RSQF_BB; i++) t[i] = t0[i];
@@ -397,15 +397,19 @@ static int rsqf_replay_rounds(uint8_t *t, const uint8_t *t0, uint32_t nbl, uint3
     const DeviceInfo &di = device_info(current_device());
     const uint32_t grid = std::min<uint32_t>((nbl + 1 + 255) / 256, di.sms * 8);
     for (int round = 0;; round++) {
-        GQF_CK(cudaMemsetAsync(ctr, 0, 3 * sizeof(uint32_t), s));  // warp list, big list, crossed
-        k_rsqf_groups<<<grid, 256, 0, s>>>(nbl, start, active, fhome, wlist, blist, ctr);
-        k_rsqf_round_warp<<<di.sms * 16, 32, 0, s>>>(t, t0, nbl, q, items, fhome, wlist, ctr, crossed, ctr + 2,
-                                                     d_ret, t0_zero ? 1 : 0);
+        GQF_CK(cudaMemsetAsync(ctr, 0, 4 * sizeof(uint32_t), s));  // three list sizes, crossed
+        k_rsqf_groups<<<grid, 256, 0, s>>>(nbl, start, active, fhome, wlist, wlist + 2 * (size_t)(nbl + 1), blist,
+                                           ctr);
+        k_rsqf_round_warp<RSQF_SMALL_GROUP, 8><<<di.sms * 8, 256, 0, s>>>(t, t0, nbl, q, items, fhome, wlist, ctr,
+                                                                        crossed, ctr + 3, d_ret, t0_zero ? 1 : 0);
+        k_rsqf_round_warp<RSQF_WARP_GROUP_MAX, 1><<<di.sms * 16, 32, 0, s>>>(
+            t, t0, nbl, q, items, fhome, wlist + 2 * (size_t)(nbl + 1), ctr + 1, crossed, ctr + 3, d_ret,
+            t0_zero ? 1 : 0);
         k_rsqf_round_big<<<std::max(1, di.sms), 64, 0, s>>>(t, t0, nbl, q, items, fhome, blist, ctr, crossed,
-                                                             ctr + 2, d_ret, t0_zero ? 1 : 0);
-        count_launches(3);
+                                                             ctr + 3, d_ret, t0_zero ? 1 : 0);
+        count_launches(4);
         uint32_t h_n = 0;
-        GQF_CK(cudaMemcpyAsync(&h_n, ctr + 2, 4, cudaMemcpyDeviceToHost, s));
+        GQF_CK(cudaMemcpyAsync(&h_n, ctr + 3, 4, cudaMemcpyDeviceToHost, s));
         GQF_CK(cudaStreamSynchronize(s));
         if (h_n == 0) return GQF_OK;
         if (round > 100000) return GQF_ERR_TIMEOUT;
@@ -438,8 +442,8 @@ int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t 
     z.take<PendFn>(nbl + 1);
     z.take<PendFn>(ntiles);
     z.take<uint32_t>(RCTL_WORDS);
-    z.take<uint32_t>(3);
-    z.take<uint32_t>(2 * (size_t)(nbl + 1));
+    z.take<uint32_t>(4);
+    z.take<uint32_t>(4 * (size_t)(nbl + 1));
     z.take<uint32_t>(2 * (size_t)(nbl + 1));
     void *basep = arena_reserve(ar, z.off);
     if (!basep) return GQF_ERR_NOMEM;
@@ -452,8 +456,8 @@ int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t 
     uint8_t *start = c.take<uint8_t>(nbl + 1), *active = c.take<uint8_t>(nbl + 1), *crossed = c.take<uint8_t>(nbl + 1),
             *sus = c.take<uint8_t>(nbl + 1);
     PendFn *fn = c.take<PendFn>(nbl + 1), *tile_fn = c.take<PendFn>(ntiles);
-    uint32_t *ctl = c.take<uint32_t>(RCTL_WORDS), *ctr = c.take<uint32_t>(3);
-    uint32_t *wlist = c.take<uint32_t>(2 * (size_t)(nbl + 1)), *blist = c.take<uint32_t>(2 * (size_t)(nbl + 1));
+    uint32_t *ctl = c.take<uint32_t>(RCTL_WORDS), *ctr = c.take<uint32_t>(4);
+    uint32_t *wlist = c.take<uint32_t>(4 * (size_t)(nbl + 1)), *blist = c.take<uint32_t>(2 * (size_t)(nbl + 1));
     int st = call_begin(ar, s, true);
     if (st) return st;
     if (n > 0) {

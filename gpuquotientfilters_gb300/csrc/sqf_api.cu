@@ -2,6 +2,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <type_traits>
 
 #include "host_common.cuh"
@@ -99,7 +101,16 @@ static size_t scatter_smem(uint32_t nb, bool pairs)
 template <typename K>
 static cudaError_t set_smem(K kernel, size_t bytes)
 {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    // the attribute is per function and device; set it only when it grows
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> done;
+    const std::pair<const void *, int> key(reinterpret_cast<const void *>(kernel), current_device());
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &cur = done[key];
+    if (bytes <= cur) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
 }
 
 // Device-side exclusive scan of bucket counts into bases (nb <= 4096).
@@ -350,8 +361,7 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
         Scratch sc = carve(base, exact ? req_exact : req, false, &bytes);
         int st = call_begin(ar, s, ms != nullptr);
         if (st) return st;
-        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
-        GQF_CK(cudaMemsetAsync(sc.fix_cnt, 0, 4, s));
+        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));  // counters, look-back, ticket, fix-ups
         BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
         if (needA) {
             st = extract_into<BPE>(qf->table, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt,
@@ -429,7 +439,15 @@ static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint3
         if (st) return st;
         TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
         BucketSrc src{sc.bitems, sc.bbase, 0, sc.bcnt};
-        k_lookup_bucketed<BPE><<<p.g.nb, LOOKUP_THREADS, 0, s>>>(src, sc.bidx, v, out);
+        const size_t lsm = lks_smem_bytes(p.g.tb);
+        const DeviceInfo &di = device_info(current_device());
+        if (BPE == 1 && (reinterpret_cast<uintptr_t>(qf->table) & 15) == 0 && p.g.tb >= 8 &&
+            lsm <= (size_t)(di.smem_optin > 0 ? di.smem_optin : 48 * 1024)) {
+            GQF_CK(set_smem(k_lookup_bucketed_s, lsm));
+            k_lookup_bucketed_s<<<p.g.nb, LKS_THREADS, lsm, s>>>(src, sc.bidx, v, p.g.tb, out);
+        } else {
+            k_lookup_bucketed<BPE><<<p.g.nb, LOOKUP_THREADS, 0, s>>>(src, sc.bidx, v, out);
+        }
         count_launches(1);
     }
     return call_end(ar, s, ms);

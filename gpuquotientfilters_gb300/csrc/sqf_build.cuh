@@ -161,14 +161,39 @@ __device__ __forceinline__ void hash_bucket_chunk(
         }
     }
     __syncthreads();
-    // s_cur[b] is now the end of bucket b's run in s_items
+    // s_cur[b] is now the end of bucket b's run in s_items.  Per bucket:
+    // item i of the run goes to out[i + delta(b)], delta(b) = base(b) +
+    // reservation(b) - start(b), and overflows the speculative stride from
+    // i = start(b) + cap - reservation(b) on (kept in s_cur).
+    {
+        constexpr uint32_t MAXPER = (4096 + THREADS - 1) / THREADS;
+        uint32_t dl[MAXPER], lim[MAXPER];
+#pragma unroll
+        for (uint32_t k = 0; k < MAXPER; k++) {
+            const uint32_t b = tid + k * THREADS;
+            if (b < g.nb) {
+                const uint32_t start = b ? s_cur[b - 1] : 0u, gb = s_gb[b];
+                const size_t base = bucket_base ? (size_t)bucket_base[b] : (size_t)b * cap;
+                dl[k] = (uint32_t)(base + gb - start);
+                lim[k] = gb >= cap ? start : (cap - gb > 0xFFFFFFFFu - start ? 0xFFFFFFFFu : start + (cap - gb));
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (uint32_t k = 0; k < MAXPER; k++) {
+            const uint32_t b = tid + k * THREADS;
+            if (b < g.nb) {
+                s_gb[b] = dl[k];
+                s_cur[b] = lim[k];
+            }
+        }
+    }
+    __syncthreads();
     for (uint32_t i = tid; i < cnt; i += THREADS) {
-        uint32_t v = s_items[i];
-        uint32_t b = v >> g.shift;
-        uint32_t start = b ? s_cur[b - 1] : 0u;
-        uint32_t gpos = s_gb[b] + (i - start);
-        if (gpos < cap) {
-            size_t dst = (bucket_base ? (size_t)bucket_base[b] : (size_t)b * cap) + gpos;
+        const uint32_t v = s_items[i];
+        const uint32_t b = v >> g.shift;
+        if (i < s_cur[b]) {
+            const uint32_t dst = i + s_gb[b];
             out[dst] = v;
             if (PAIRS) out_idx[dst] = s_idx[i];
         } else {
@@ -480,7 +505,46 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
     // items are read in batches of LB per thread so LB loads are in flight
     constexpr int LB = 8;
 
-    if (bitmap) {
+    if (bitmap && na == 0 && a.op != OP_DELETE && ((bbase & 3) == 0)) {
+        // build from one 16-byte aligned source (the speculative bucket
+        // stride keeps bucket starts aligned): the first four items per
+        // thread as one 16-byte load issued before the masks are cleared,
+        // the rest four at a time
+        const uint4 *src4 = reinterpret_cast<const uint4 *>(a.B.items + bbase);
+        const uint32_t n4 = nbn >> 2;
+        auto put = [&](uint32_t v) {
+            atomicOr(s_mask + mask_word((v >> a.r) & (S - 1)), 1u << (v & rmask));
+        };
+        constexpr int LV = 4;  // 16-byte loads in flight per thread
+        uint4 w[LV];
+#pragma unroll
+        for (int k = 0; k < LV; k++) {
+            const uint32_t j = k * THREADS + tid;
+            w[k] = j < n4 ? __ldg(src4 + j) : make_uint4(0, 0, 0, 0);
+        }
+        for (uint32_t i = tid; i < (S + S / 8) / 4; i += THREADS)
+            reinterpret_cast<uint4 *>(s_mask)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        for (uint32_t j0 = 0;; j0 += LV * THREADS) {
+#pragma unroll
+            for (int k = 0; k < LV; k++) {
+                if (j0 + k * THREADS + tid < n4) {
+                    put(w[k].x);
+                    put(w[k].y);
+                    put(w[k].z);
+                    put(w[k].w);
+                }
+            }
+            if (j0 + LV * THREADS >= n4) break;
+#pragma unroll
+            for (int k = 0; k < LV; k++) {
+                const uint32_t j = j0 + LV * THREADS + k * THREADS + tid;
+                w[k] = j < n4 ? __ldg(src4 + j) : make_uint4(0, 0, 0, 0);
+            }
+        }
+        for (uint32_t i = (n4 << 2) + tid; i < nbn; i += THREADS) put(a.B.items[bbase + i]);  // tail
+        __syncthreads();
+    } else if (bitmap) {
         // A: remainder sets by quotient (A first, then B); mask of local
         // quotient x lives at word mask_word(x) (one pad uint4 per 8)
         for (uint32_t i = tid; i < (S + S / 8) / 4; i += THREADS)

@@ -243,52 +243,69 @@ __device__ __forceinline__ Counts3 block_excl3(Counts3 c)
     return r;
 }
 
+// Copies a tile's outputs, staged in shared memory in output order, to
+// out[base .. base + cnt) with coalesced stores.
+__device__ __forceinline__ void flush_tile(const uint32_t *s_out, uint32_t cnt, uint32_t *__restrict__ out,
+                                           uint32_t base)
+{
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt; i += EXTRACT_THREADS) out[base + i] = s_out[i];
+}
+
 // Pass 2: positions of occupied slots, in slot order (Q[j] = quotient of
-// the j-th run).
+// the j-th run).  A tile's entries are staged in shared memory and stored
+// coalesced.
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_occ_list(const uint8_t *__restrict__ t, uint32_t nslots,
                                                              uint32_t nbytes, const Counts3 *__restrict__ tiles,
                                                              uint32_t *__restrict__ Q)
 {
+    __shared__ uint32_t s_out[EXTRACT_TILE];
     ThreadSlots<BPE> ts;
     ts.load(t, nslots, nbytes);
-    Counts3 ex = block_excl3(ts.totals());
-    uint32_t o = tiles[blockIdx.x].occ + ex.occ;
+    const Counts3 ex = block_excl3(ts.totals());
+    uint32_t o = ex.occ;
 #pragma unroll
     for (int w = 0; w < EXTRACT_WPT; w++) {
         uint32_t m = ts.occ[w];
         while (m) {
-            int k = __ffs(m) - 1;
+            const int k = __ffs(m) - 1;
             m &= m - 1;
-            Q[o++] = ts.s0 + 8 * w + k;
+            s_out[o++] = ts.s0 + 8 * w + k;
         }
     }
+    const uint32_t base = tiles[blockIdx.x].occ;
+    flush_tile(s_out, tiles[blockIdx.x + 1].occ - base, Q, base);
 }
 
-// Pass 3: E[i] = fingerprint of the i-th stored element.
+// Pass 3: E[i] = fingerprint of the i-th stored element (staged per tile,
+// stored coalesced).
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_extract(const uint8_t *__restrict__ t, uint32_t nslots,
                                                             uint32_t nbytes, uint32_t r,
                                                             const Counts3 *__restrict__ tiles,
                                                             const uint32_t *__restrict__ Q, uint32_t *__restrict__ E)
 {
+    __shared__ uint32_t s_out[EXTRACT_TILE];
     ThreadSlots<BPE> ts;
     ts.load(t, nslots, nbytes);
-    Counts3 ex = block_excl3(ts.totals());
-    uint32_t o = tiles[blockIdx.x].ne + ex.ne;
+    const Counts3 ex = block_excl3(ts.totals());
+    uint32_t o = ex.ne;
     uint32_t runs_before = tiles[blockIdx.x].rs + ex.rs;  // run starts strictly before this thread's slots
 #pragma unroll
     for (int w = 0; w < EXTRACT_WPT; w++) {
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             if (!((ts.ne[w] >> k) & 1u)) continue;
-            uint32_t rs_upto = runs_before + __popc(ts.rs[w] & ((2u << k) - 1u));
+            const uint32_t rs_upto = runs_before + __popc(ts.rs[w] & ((2u << k) - 1u));
             // rs_upto >= 1 in a valid table (the first element of a cluster starts a run)
-            uint32_t j = rs_upto ? rs_upto - 1 : 0;
-            E[o++] = (Q[j] << r) | (ts.e[w][k] >> 3);
+            const uint32_t j = rs_upto ? rs_upto - 1 : 0;
+            s_out[o++] = (Q[j] << r) | (ts.e[w][k] >> 3);
         }
         runs_before += __popc(ts.rs[w]);
     }
+    const uint32_t base = tiles[blockIdx.x].ne;
+    flush_tile(s_out, tiles[blockIdx.x + 1].ne - base, E, base);
 }
 
 // Bucket bounds of a sorted fingerprint list: base[b] = lower_bound(b << shift).

@@ -227,4 +227,151 @@ __global__ void __launch_bounds__(LOOKUP_THREADS) k_lookup_bucketed(BucketSrc sr
     }
 }
 
+// ---------------------------------------------------------------------------
+// Sorted lookups, one-byte slots, from a shared-memory image of the bucket.
+// A bucket's queries all have quotients in [x0, x0 + 2^tb).  The CTA stages
+// the table slice [x0, x0 + 2^tb + LKS_MARGIN) once, and indexes it once:
+// per 8-slot word the occupied mask and the occupied count before it, and
+// the list of run starts in slot order.  Runs are stored in quotient order,
+// one per occupied quotient, so the run of the j-th occupied quotient at or
+// past x0 is run start number D0 + j, where D0 counts the runs of quotients
+// below x0 still pending at x0 (the walk-back of sqf_query_b1 for slot x0,
+// done once per bucket).  A query then costs a few shared-memory reads and a
+// short scan of its run; a run starting or ending outside the staged slice
+// falls back to sqf_query_b1 on the table.  Results equal sqf_query_b1's on
+// every valid table.
+// ---------------------------------------------------------------------------
+constexpr int LKS_THREADS = 256;
+constexpr uint32_t LKS_MARGIN = 2048;
+
+__host__ __device__ inline size_t lks_smem_bytes(uint32_t tb)
+{
+    const size_t L = ((size_t)1 << tb) + LKS_MARGIN;  // slots staged
+    const size_t W = L / 8;                            // 8-slot words
+    return L + 2 * W + W + 2 * L + 64;                 // bytes, occupied prefix, masks, run starts
+}
+
+static __global__ void __launch_bounds__(LKS_THREADS) k_lookup_bucketed_s(BucketSrc src, const uint32_t *__restrict__ idx,
+                                                                  TableView v, uint32_t tb,
+                                                                  uint32_t *__restrict__ out)
+{
+    extern __shared__ __align__(16) uint8_t smem_lks[];
+    const uint32_t S = 1u << tb, L = S + LKS_MARGIN, W = L / 8;
+    uint8_t *s_tab = smem_lks;
+    uint16_t *s_occp = reinterpret_cast<uint16_t *>(s_tab + L);
+    uint8_t *s_occ8 = reinterpret_cast<uint8_t *>(s_occp + W);
+    uint16_t *s_rs = reinterpret_cast<uint16_t *>(s_occ8 + ((W + 1) & ~1u));
+    __shared__ uint32_t s_wsum[2][LKS_THREADS / 32];
+    __shared__ int s_D0;
+    __shared__ uint32_t s_nrs;
+    const uint32_t b = blockIdx.x, n = src.count(b);
+    if (n == 0) return;
+    const size_t base = src.start(b);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t x0 = b << tb;
+    // stage slots [x0, x0 + L), zero past the table
+    for (uint32_t i = tid * 16; i < L; i += LKS_THREADS * 16) {
+        uint4 w4;
+        if ((size_t)x0 + i + 16 <= v.nbytes) {
+            w4 = __ldg(reinterpret_cast<const uint4 *>(v.t + x0 + i));
+        } else {
+            uint8_t tmp[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) tmp[k] = (size_t)x0 + i + k < v.nbytes ? v.t[x0 + i + k] : 0;
+            w4 = *reinterpret_cast<uint4 *>(tmp);
+        }
+        *reinterpret_cast<uint4 *>(s_tab + i) = w4;
+    }
+    if (tid == 0) {
+        // runs of quotients below x0 still pending at x0 (sqf_query_b1's
+        // walk back for slot x0)
+        int D = 0;
+        const Flags8 f0 = flags8(ld_word(v, x0 >> 3));
+        if (f0.shift & 1u) {
+            for (int ww = (int)(x0 >> 3) - 1; ww >= 0; ww--) {
+                const Flags8 g = flags8(ld_word(v, (uint32_t)ww));
+                const uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
+                if (cs2) {
+                    const uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
+                    D += popc32(g.occ & rng) - popc32(rs2 & rng);
+                    break;
+                }
+                D += popc32(g.occ) - popc32(rs2);
+            }
+        }
+        s_D0 = D;
+    }
+    __syncthreads();
+    // index: this thread's words [w0, w1)
+    const uint32_t per = (W + LKS_THREADS - 1) / LKS_THREADS;
+    const uint32_t w0 = min(W, tid * per), w1 = min(W, w0 + per);
+    uint32_t nocc = 0, nrs = 0;
+    for (uint32_t w = w0; w < w1; w++) {
+        const Flags8 f = flags8(*reinterpret_cast<const uint64_t *>(s_tab + 8 * w));
+        nocc += popc32(f.occ);
+        nrs += popc32(f.nonempty & ~f.cont);
+    }
+    uint32_t io = nocc, ir = nrs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, io, o), c = __shfl_up_sync(0xffffffffu, ir, o);
+        if (lane >= o) {
+            io += a;
+            ir += c;
+        }
+    }
+    if (lane == 31) {
+        s_wsum[0][wid] = io;
+        s_wsum[1][wid] = ir;
+    }
+    __syncthreads();
+    uint32_t po = io - nocc, pr = ir - nrs;
+    for (int w = 0; w < wid; w++) {
+        po += s_wsum[0][w];
+        pr += s_wsum[1][w];
+    }
+    if (tid == LKS_THREADS - 1) s_nrs = pr + nrs;
+    for (uint32_t w = w0; w < w1; w++) {
+        const Flags8 f = flags8(*reinterpret_cast<const uint64_t *>(s_tab + 8 * w));
+        s_occp[w] = (uint16_t)po;
+        s_occ8[w] = (uint8_t)f.occ;
+        po += popc32(f.occ);
+        for (uint32_t m = f.nonempty & ~f.cont & 0xFFu; m; m &= m - 1u) s_rs[pr++] = (uint16_t)(8 * w + lowest_bit(m));
+    }
+    __syncthreads();
+    const int D0 = s_D0;
+    const uint32_t nrs_all = s_nrs;
+    const uint32_t qmask = (1u << v.q) - 1u, rmask = (1u << v.r) - 1u;
+    for (uint32_t i = tid; i < n; i += LKS_THREADS) {
+        const uint32_t fp = src.items[base + i], qi = idx[base + i];
+        const uint32_t fq = (fp >> v.r) & qmask, fr = fp & rmask;
+        const uint32_t lq = fq - x0, w = lq >> 3, k = lq & 7u;
+        const uint32_t m8 = s_occ8[w];
+        uint32_t res = GQF_NOT_FOUND;
+        if ((m8 >> k) & 1u) {
+            const int rk = D0 + (int)s_occp[w] + popc32(m8 & ((1u << k) - 1u));
+            bool fallback = rk < 0 || (uint32_t)rk >= nrs_all;
+            if (!fallback) {
+                uint32_t p = s_rs[rk];
+                for (;;) {
+                    const uint32_t e = s_tab[p];
+                    const uint32_t rem = e >> 3;
+                    if (rem == fr) {
+                        res = x0 + p;
+                        break;
+                    }
+                    if (rem > fr) break;
+                    if (++p >= L) {
+                        fallback = true;
+                        break;
+                    }
+                    if (!((s_tab[p] >> 1) & 1u)) break;
+                }
+            }
+            if (fallback) res = sqf_query_b1(v, fq, fr, ld_word(v, fq >> 3));
+        }
+        out[qi] = res;
+    }
+}
+
 }  // namespace gqf
