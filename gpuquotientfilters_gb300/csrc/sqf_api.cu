@@ -133,6 +133,8 @@ struct Scratch {
     uint32_t *ticket;
     uint32_t *fix_cnt;
     uint32_t *a_dups;  // table holds duplicate fingerprints (set by extraction)
+    uint32_t *fused_fail;  // the in-place update could not decode some bucket
+    uint8_t *snap;         // table snapshot of the in-place update
     uint32_t *bbase;  // nb+1: exact batch bases
     uint32_t *fix_list;
     uint32_t fix_cap;
@@ -152,6 +154,7 @@ struct ScratchReq {
     bool extract;   // table contents needed
     bool extract2;  // second table (merge)
     uint32_t nslots;
+    size_t snap_bytes = 0;  // in-place update: snapshot of the table
 };
 
 static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *bytes_out)
@@ -164,6 +167,7 @@ static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *
         s.ticket = c.template take<uint32_t>(1, 4);
         s.fix_cnt = c.template take<uint32_t>(1, 4);
         s.a_dups = c.template take<uint32_t>(1, 4);
+        s.fused_fail = c.template take<uint32_t>(1, 4);
         s.ctrl_bytes = c.off;
         s.bbase = c.template take<uint32_t>(nb + 1);
         s.fix_cap = std::max<uint32_t>(65536u, r.nslots / 8);
@@ -183,6 +187,7 @@ static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *
                 s.a2cnt = c.template take<uint32_t>(nb);
             }
         }
+        s.snap = r.snap_bytes ? c.template take<uint8_t>(r.snap_bytes) : nullptr;
     };
     if (sizing_only) {
         Sizer z;
@@ -251,7 +256,7 @@ static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, S
 template <int BPE>
 static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table, const BucketSrc &A,
                          const BucketSrc &B, int op, int nodup, bool bitmap_ok, const uint32_t *a_dups, Scratch &sc,
-                         uint32_t *err, cudaStream_t s)
+                         uint32_t *err, cudaStream_t s, const uint8_t *src_table = nullptr)
 {
     // slots past the last bucket's quotients only receive spill: clear them
     size_t tail = (size_t)(1u << tg.q) * BPE;
@@ -276,12 +281,15 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
     a.fix_cnt = sc.fix_cnt;
     a.fix_cap = sc.fix_cap;
     a.err = err;
+    a.src_table = src_table;
+    a.fused_fail = src_table ? sc.fused_fail : nullptr;
+    const size_t smem = p.smem + (src_table ? layout_fused_bytes(p.g.tb) + 16 : 0);
     // one thread per 32 consecutive quotients (fewer per thread below 1024
     // quotients per bucket)
     cudaError_t e = cudaSuccess;
     auto go = [&](auto kernel, int threads) {
-        e = set_smem(kernel, p.smem);
-        if (e == cudaSuccess) kernel<<<p.g.nb, threads, p.smem, s>>>(a);
+        e = set_smem(kernel, smem);
+        if (e == cudaSuccess) kernel<<<p.g.nb, threads, smem, s>>>(a);
     };
     switch (p.g.tb) {
     case 15: go(k_bucket_layout<1024, 32, BPE>, 1024); break;
@@ -350,8 +358,46 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
     ScratchReq req_exact = req;
     req_exact.batch_items = std::max<size_t>(n, 1);
     carve(nullptr, req_exact, true, &bytes_exact);
-    void *base = arena_reserve(ar, std::max(bytes, bytes_exact));
+    // In-place update: a synchronous insert or delete on one-byte slots
+    // with set semantics decodes every bucket's old contents straight from
+    // a snapshot of the table (no extraction pass, see LayoutArgs).  If a
+    // bucket cannot be decoded that way (a table holding duplicate
+    // fingerprints), the table is restored from the snapshot and the op
+    // reruns the general way below.
+    const bool fused = BPE == 1 && bitmap_ok && (op == OP_INSERT || op == OP_DELETE) && ms && !bFromTable;
+    ScratchReq req_fused = req_exact;
+    req_fused.snap_bytes = tg.T;
+    size_t bytes_fused = 0;
+    if (fused) carve(nullptr, req_fused, true, &bytes_fused);
+    void *base = arena_reserve(ar, std::max(std::max(bytes, bytes_exact), bytes_fused));
     if (!base) return GQF_ERR_NOMEM;
+    float ms_fused = 0.0f;
+    if (fused) {
+        Scratch sc = carve(base, req_fused, false, &bytes);
+        int st = call_begin(ar, s, true);
+        if (st) return st;
+        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
+        GQF_CK(cudaMemcpyAsync(sc.snap, qf->table, tg.T, cudaMemcpyDeviceToDevice, s));
+        BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
+        if (n) {
+            st = bucket_batch(keys, n, p, sc, true, false, ar.err, s);
+            if (st) return st;
+            B = BucketSrc{sc.bitems, sc.bbase, 0, sc.bcnt};
+        }
+        st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, true, nullptr, sc, ar.err, s, sc.snap);
+        if (st) return st;
+        GQF_CK(cudaEventRecord(ar.ev1, s));
+        GQF_CK(cudaEventSynchronize(ar.ev1));
+        uint32_t e = 0, fail = 0;
+        GQF_CK(cudaMemcpy(&e, ar.err, 4, cudaMemcpyDeviceToHost));
+        GQF_CK(cudaMemcpy(&fail, sc.fused_fail, 4, cudaMemcpyDeviceToHost));
+        GQF_CK(cudaEventElapsedTime(&ms_fused, ar.ev0, ar.ev1));
+        if (!fail) {
+            *ms = ms_fused;
+            return dev_err_to_status(e);
+        }
+        GQF_CK(cudaMemcpy(qf->table, sc.snap, tg.T, cudaMemcpyDeviceToDevice));
+    }
     // A timed build uses speculative bucket strides (one pass over the keys)
     // and reruns with exact bucket bases if a bucket overflowed; the rerun
     // rewrites the whole table from the keys.  Updates read the table, so
@@ -393,6 +439,7 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
             continue;
         }
         GQF_CK(cudaEventElapsedTime(ms, ar.ev0, ar.ev1));
+        *ms += ms_fused;
         return dev_err_to_status(e);
     }
     return GQF_ERR_FULL;

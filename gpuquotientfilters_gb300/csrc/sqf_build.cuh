@@ -413,6 +413,13 @@ struct LayoutArgs {
     uint32_t *fix_cnt;
     uint32_t fix_cap;
     uint32_t *err;
+    // In-place update (insert / delete, one-byte slots, bitmap mode): A is
+    // decoded bucket by bucket from this snapshot of the table taken before
+    // the op, instead of from an extracted list.  A bucket it cannot decode
+    // here (duplicate or out-of-order remainders, runs past its staged
+    // slice) sets *fused_fail and the host reruns the op the general way.
+    const uint8_t *src_table = nullptr;
+    uint32_t *fused_fail = nullptr;
 };
 
 // Shared-memory plan of k_bucket_layout: region 0 holds either the
@@ -431,6 +438,15 @@ __host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_it
     size_t r0 = (layout_region0_bytes(tb, cap_items, bpe, bitmap) + 15) & ~(size_t)15;
     size_t tile = (((S + SPILL_SLOTS) * bpe + 32) + 15) & ~(size_t)15;
     return r0 + tile + S / 8;  // + occupied bit per quotient
+}
+// Extra shared memory of the in-place update decode: per 32-slot word of
+// the staged slice its run-start mask and the run starts before it, per
+// 32-quotient word of the bucket its occupied mask and the count before it.
+__host__ __device__ inline size_t layout_fused_bytes(uint32_t tb)
+{
+    const size_t S = (size_t)1 << tb, LW = (S + SPILL_SLOTS) / 32, QW = S / 32;
+    return ((LW * 4 + 15) & ~(size_t)15) + ((LW * 2 + 15) & ~(size_t)15) + ((QW * 4 + 15) & ~(size_t)15) +
+           ((QW * 2 + 15) & ~(size_t)15);
 }
 
 // Group walk (general mode): quotients [qb, qb+QPT) in slot order, calling
@@ -466,7 +482,7 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
     using Rem = typename std::conditional<BPE == 1, uint8_t, uint16_t>::type;
     extern __shared__ __align__(16) uint8_t smem_layout[];
     const uint32_t S = 1u << a.tb;
-    const bool bitmap = BPE == 1 && a.bitmap_ok && !(a.a_dups && *a.a_dups);
+    const bool bitmap = BPE == 1 && a.bitmap_ok && (a.src_table || !(a.a_dups && *a.a_dups));
     uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem_layout);   // general: u16 counters
     uint32_t *s_mask = reinterpret_cast<uint32_t *>(smem_layout);  // bitmap: u32 per local quotient
     Rem *s_rem = reinterpret_cast<Rem *>(smem_layout + 4 * ((size_t)S / 2 + S / 32 + 8));
@@ -505,7 +521,186 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
     // items are read in batches of LB per thread so LB loads are in flight
     constexpr int LB = 8;
 
-    if (bitmap && na == 0 && a.op != OP_DELETE && ((bbase & 3) == 0)) {
+    if (BPE == 1 && bitmap && a.src_table) {
+        // In-place update: decode this bucket's old contents from the
+        // snapshot.  Runs are stored in quotient order, one per occupied
+        // quotient; the runs starting at or past x0 are first the D0 still
+        // pending from quotients below x0, then those of the bucket's
+        // occupied quotients in order.
+        const uint32_t L = BUF;
+        uint8_t *s_sl = s_tile;  // the slice, in the tile buffer until the emit
+        uint8_t *fx = smem_layout + ((layout_smem_bytes(a.tb, a.cap_items, BPE, true) + 15) & ~(size_t)15);
+        const size_t o1 = ((size_t)(L / 32) * 4 + 15) & ~(size_t)15, o2 = ((size_t)(L / 32) * 2 + 15) & ~(size_t)15,
+                     o3 = ((size_t)(S / 32) * 4 + 15) & ~(size_t)15;
+        uint32_t *s_rs32 = reinterpret_cast<uint32_t *>(fx);
+        uint16_t *s_rsp = reinterpret_cast<uint16_t *>(fx + o1);
+        uint32_t *s_oc32 = reinterpret_cast<uint32_t *>(fx + o1 + o2);
+        uint16_t *s_ocp = reinterpret_cast<uint16_t *>(fx + o1 + o2 + o3);
+        __shared__ int s_D0;
+        __shared__ uint32_t s_nrs;
+        for (uint32_t i = tid; i < (S + S / 8) / 4; i += THREADS)
+            reinterpret_cast<uint4 *>(s_mask)[i] = make_uint4(0, 0, 0, 0);
+        const uint8_t *src = a.src_table;
+        for (uint32_t i = tid * 16; i < L; i += THREADS * 16) {
+            uint4 w4;
+            if ((size_t)x0 + i + 16 <= a.nslots) {
+                w4 = __ldg(reinterpret_cast<const uint4 *>(src + x0 + i));
+            } else {
+                uint8_t tmp[16];
+#pragma unroll
+                for (int k = 0; k < 16; k++) tmp[k] = (size_t)x0 + i + k < a.nslots ? src[x0 + i + k] : 0;
+                w4 = *reinterpret_cast<uint4 *>(tmp);
+            }
+            *reinterpret_cast<uint4 *>(s_sl + i) = w4;
+        }
+        if (tid == 0) {
+            // runs of quotients below x0 still pending at x0: the lookup's
+            // walk back to the cluster start, for slot x0
+            int D = 0;
+            if (x0 > 0 && (src[x0] & 1u)) {
+                for (int ww = (int)(x0 >> 3) - 1; ww >= 0; ww--) {
+                    const Flags8 g = flags8(__ldg(reinterpret_cast<const unsigned long long *>(src) + ww));
+                    const uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
+                    if (cs2) {
+                        const uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
+                        D += popc32(g.occ & rng) - popc32(rs2 & rng);
+                        break;
+                    }
+                    D += popc32(g.occ) - popc32(rs2);
+                }
+            }
+            s_D0 = D;
+        }
+        __syncthreads();
+        // 32-slot masks: run starts over the slice, occupied over the bucket
+        for (uint32_t w = tid; w < L / 32; w += THREADS) {
+            uint32_t rsm = 0, ocm = 0;
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const Flags8 f = flags8(*reinterpret_cast<const uint64_t *>(s_sl + 32 * w + 8 * h));
+                rsm |= ((f.nonempty & ~f.cont) & 0xFFu) << (8 * h);
+                ocm |= (f.occ & 0xFFu) << (8 * h);
+            }
+            s_rs32[w] = rsm;
+            if (w < S / 32) s_oc32[w] = ocm;
+        }
+        __syncthreads();
+        // exclusive prefix counts: thread-contiguous word ranges + block scan
+        {
+            const uint32_t per = (L / 32 + THREADS - 1) / THREADS;
+            const uint32_t w0 = min(L / 32, tid * per), w1 = min(L / 32, w0 + per);
+            uint32_t cr = 0, co = 0;
+            for (uint32_t w = w0; w < w1; w++) {
+                cr += __popc(s_rs32[w]);
+                if (w < S / 32) co += __popc(s_oc32[w]);
+            }
+            uint32_t ir = cr, io = co;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xffffffffu, ir, o), y = __shfl_up_sync(0xffffffffu, io, o);
+                if (lane >= o) {
+                    ir += x;
+                    io += y;
+                }
+            }
+            if (lane == 31) {
+                s_wfn[wid].n = ir;
+                s_wfn[wid].F = io;
+            }
+            __syncthreads();
+            uint32_t pr = ir - cr, po = io - co;
+            for (int w = 0; w < wid; w++) {
+                pr += s_wfn[w].n;
+                po += s_wfn[w].F;
+            }
+            if (tid == THREADS - 1) s_nrs = pr + cr;  // run starts in the slice
+            for (uint32_t w = w0; w < w1; w++) {
+                s_rsp[w] = (uint16_t)pr;
+                pr += __popc(s_rs32[w]);
+                if (w < S / 32) {
+                    s_ocp[w] = (uint16_t)po;
+                    po += __popc(s_oc32[w]);
+                }
+            }
+        }
+        // the batch: its remainders, per quotient, into the bitmaps
+        for (uint32_t i0 = 0; i0 < nbn; i0 += THREADS * LB) {
+            uint32_t v[LB];
+#pragma unroll
+            for (int k = 0; k < LB; k++) {
+                const uint32_t i = i0 + k * THREADS + tid;
+                v[k] = i < nbn ? a.B.items[bbase + i] : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < LB; k++)
+                if (i0 + k * THREADS + tid < nbn)
+                    atomicOr(s_mask + mask_word((v[k] >> a.r) & (S - 1)), 1u << (v[k] & rmask));
+        }
+        __syncthreads();
+        {
+            // each thread decodes the runs of its own QPT quotients: the run
+            // of its first occupied quotient is run start number D0 + (the
+            // bucket's occupied quotients before qb); later ones follow in
+            // slot order.  Then per quotient: old set | batch (insert) or
+            // old set & ~batch (delete).
+            const int D0 = s_D0;
+            const int nrs = (int)s_nrs;
+            const uint32_t qw = qb >> 5, qs = qb & 31;
+            const uint32_t ocm = (s_oc32[qw] >> qs) & (QPT >= 32 ? 0xFFFFFFFFu : ((1u << (QPT & 31)) - 1u));
+            const int j0 = (int)s_ocp[qw] + __popc(s_oc32[qw] & ((1u << qs) - 1u));
+            const bool del = a.op == OP_DELETE;
+            bool bad = false;
+            uint32_t pos = 0;  // current run start (slot of the slice)
+            if (ocm) {
+                const int k = D0 + j0;
+                if (k < 0 || k >= nrs) {
+                    bad = true;
+                } else {
+                    uint32_t lo = 0, hi = L / 32;  // last word with s_rsp[w] <= k
+                    while (hi - lo > 1) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if ((int)s_rsp[mid] <= k) lo = mid;
+                        else hi = mid;
+                    }
+                    pos = (lo << 5) + (uint32_t)select_bit(s_rs32[lo], k - (int)s_rsp[lo]);
+                }
+            }
+            bool first = true;
+#pragma unroll 4
+            for (uint32_t jq = 0; jq < QPT; jq++) {
+                uint32_t am = 0;
+                if (((ocm >> jq) & 1u) && !bad) {
+                    if (!first) {  // the next run start, at or past the previous run's end
+                        uint32_t w = pos >> 5;
+                        uint32_t mm = pos < L ? (s_rs32[w] & ~((1u << (pos & 31)) - 1u)) : 0u;
+                        while (!mm && ++w < L / 32) mm = s_rs32[w];
+                        if (!mm) bad = true;
+                        else pos = (w << 5) + (uint32_t)(__ffs(mm) - 1);
+                    }
+                    first = false;
+                    if (!bad) {
+                        int prev = -1;
+                        for (;;) {
+                            const uint32_t rem = (uint32_t)s_sl[pos] >> 3;
+                            if ((int)rem <= prev) bad = true;  // duplicate or unsorted run
+                            prev = (int)rem;
+                            am |= 1u << rem;
+                            if (++pos >= L) {
+                                bad = true;  // the run may continue past the slice
+                                break;
+                            }
+                            const uint32_t e2 = s_sl[pos];
+                            if (!((e2 & 7u) && (e2 & 2u))) break;
+                        }
+                    }
+                }
+                uint32_t *mw = s_mask + mask_word(qb + jq);
+                *mw = del ? (am & ~*mw) : (am | *mw);
+            }
+            if (bad) atomicOr(a.fused_fail, 1u);
+        }
+        __syncthreads();
+    } else if (bitmap && na == 0 && a.op != OP_DELETE && ((bbase & 3) == 0)) {
         // build from one 16-byte aligned source (the speculative bucket
         // stride keeps bucket starts aligned): the first four items per
         // thread as one 16-byte load issued before the masks are cleared,
