@@ -291,16 +291,30 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
         e = set_smem(kernel, smem);
         if (e == cudaSuccess) kernel<<<p.g.nb, threads, smem, s>>>(a);
     };
-    switch (p.g.tb) {
-    case 15: go(k_bucket_layout<1024, 32, BPE>, 1024); break;
-    case 14: go(k_bucket_layout<512, 32, BPE>, 512); break;
-    case 13: go(k_bucket_layout<256, 32, BPE>, 256); break;
-    case 12: go(k_bucket_layout<128, 32, BPE>, 128); break;
-    case 11: go(k_bucket_layout<64, 32, BPE>, 64); break;
-    case 10: go(k_bucket_layout<32, 32, BPE>, 32); break;
-    case 9: go(k_bucket_layout<32, 16, BPE>, 32); break;
-    case 8: go(k_bucket_layout<32, 8, BPE>, 32); break;
-    default: go(k_bucket_layout<32, 4, BPE>, 32); break;
+    if (src_table && BPE == 1) {
+        switch (p.g.tb) {
+        case 15: go(k_bucket_layout<1024, 32, BPE, true>, 1024); break;
+        case 14: go(k_bucket_layout<512, 32, BPE, true>, 512); break;
+        case 13: go(k_bucket_layout<256, 32, BPE, true>, 256); break;
+        case 12: go(k_bucket_layout<128, 32, BPE, true>, 128); break;
+        case 11: go(k_bucket_layout<64, 32, BPE, true>, 64); break;
+        case 10: go(k_bucket_layout<32, 32, BPE, true>, 32); break;
+        case 9: go(k_bucket_layout<32, 16, BPE, true>, 32); break;
+        case 8: go(k_bucket_layout<32, 8, BPE, true>, 32); break;
+        default: go(k_bucket_layout<32, 4, BPE, true>, 32); break;
+        }
+    } else {
+        switch (p.g.tb) {
+        case 15: go(k_bucket_layout<1024, 32, BPE>, 1024); break;
+        case 14: go(k_bucket_layout<512, 32, BPE>, 512); break;
+        case 13: go(k_bucket_layout<256, 32, BPE>, 256); break;
+        case 12: go(k_bucket_layout<128, 32, BPE>, 128); break;
+        case 11: go(k_bucket_layout<64, 32, BPE>, 64); break;
+        case 10: go(k_bucket_layout<32, 32, BPE>, 32); break;
+        case 9: go(k_bucket_layout<32, 16, BPE>, 32); break;
+        case 8: go(k_bucket_layout<32, 8, BPE>, 32); break;
+        default: go(k_bucket_layout<32, 4, BPE>, 32); break;
+        }
     }
     GQF_CK(e);
     const DeviceInfo &di = device_info(current_device());

@@ -476,7 +476,9 @@ __device__ __forceinline__ void walk_groups(const uint32_t *s_cnt, const Rem *s_
 // K2: one CTA per bucket (taken in ticket order for the look-back).
 // ---------------------------------------------------------------------
 // THREADS threads own QPT consecutive quotients each (S = THREADS * QPT).
-template <int THREADS, int QPT_, int BPE>
+// FUSED instantiations carry the in-place update decode (LayoutArgs::
+// src_table); the others compile without it.
+template <int THREADS, int QPT_, int BPE, bool FUSED = false>
 __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const uint32_t b)
 {
     using Rem = typename std::conditional<BPE == 1, uint8_t, uint16_t>::type;
@@ -521,7 +523,7 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
     // items are read in batches of LB per thread so LB loads are in flight
     constexpr int LB = 8;
 
-    if (BPE == 1 && bitmap && a.src_table) {
+    if (FUSED && BPE == 1 && bitmap && a.src_table) {
         // In-place update: decode this bucket's old contents from the
         // snapshot.  Runs are stored in quotient order, one per occupied
         // quotient; the runs starting at or past x0 are first the D0 still
@@ -1065,13 +1067,13 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
 
 // One CTA per bucket, taken in ticket order so every bucket's predecessors
 // are running or done when it looks back.
-template <int THREADS, int QPT_, int BPE>
+template <int THREADS, int QPT_, int BPE, bool FUSED = false>
 __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_layout(LayoutArgs a)
 {
     __shared__ uint32_t s_ticket;
     if (threadIdx.x == 0) s_ticket = atomicAdd(a.ticket, 1u);
     __syncthreads();
-    bucket_layout_body<THREADS, QPT_, BPE>(a, s_ticket);
+    bucket_layout_body<THREADS, QPT_, BPE, FUSED>(a, s_ticket);
 }
 
 template <int BPE>
