@@ -33,6 +33,10 @@ N_KEYS = 53687091
 N_LOOKUP = 1 << 24
 N_INSERT = 1 << 20
 N_DELETE = 1 << 20
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one q=26 r=5 NoDup build of
+# N_KEYS keys, from one `ncu --set full` capture: k_hash_bucket 384,808,192 + k_bucket_layout
+# 261,271,808 (k_fixup_occ touches a few KB).
+BUILD_DRAM_BYTES = 384808192 + 261271808
 
 
 def peaks():
@@ -222,7 +226,9 @@ def run_gpu(args, world, rank, local):
         "batched": batched, "served": served,
         "roofline": {"bound": "hbm", "kernel": "bulk build pipeline (hash+bucket scatter, bucket layout, fixup)",
                      "achieved": b["alg_GBps"], "peak": peak, "unit": "GB/s", "frac": b["frac_hbm"],
-                     "traffic": None, "peak_source": peak_kind},
+                     "traffic": BUILD_DRAM_BYTES if q == Q else None,
+                     "traffic_source": "ncu capture of the same build (k_hash_bucket + k_bucket_layout)",
+                     "peak_source": peak_kind},
     }
 
 
