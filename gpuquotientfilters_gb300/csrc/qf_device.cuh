@@ -89,16 +89,53 @@ QF_HD int select_bit(uint32_t m, int j)
     return lowest_bit(m);
 }
 
-// ---- memory-order helpers for the decoupled look-back -------------------
-#ifdef __CUDACC__
-__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+// ---- byte-lane SWAR: one flag bit per byte of a u64 (slot k = byte k) ---
+constexpr uint64_t BL_LO = 0x0101010101010101ull;  // bit 0 of every byte
+constexpr uint64_t BL_HI = 0x8080808080808080ull;  // bit 7 of every byte
+// bytes [0, n) set; n in [0, 8]
+QF_HD uint64_t bytes_below(uint32_t n) { return n >= 8 ? ~0ull : ((1ull << (8 * n)) - 1ull); }
+QF_HD int popc64(uint64_t x)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+#ifdef __CUDA_ARCH__
+    return __popcll(x);
+#else
+    return __builtin_popcountll(x);
+#endif
 }
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+QF_HD uint32_t lowest_byte(uint64_t x)  // x != 0
+{
+#ifdef __CUDA_ARCH__
+    return (uint32_t)(__ffsll((long long)x) - 1) >> 3;
+#else
+    return (uint32_t)__builtin_ctzll(x) >> 3;
+#endif
+}
+QF_HD uint32_t highest_byte(uint64_t x)  // x != 0
+{
+#ifdef __CUDA_ARCH__
+    return (uint32_t)(63 - __clzll((long long)x)) >> 3;
+#else
+    return (uint32_t)(63 - __builtin_clzll(x)) >> 3;
+#endif
+}
+// per-slot flags of 8 one-byte slots, bit 0 of each byte
+QF_HD uint64_t bl_unshifted(uint64_t x) { return ~x & BL_LO; }
+// run starts: non-empty (metadata != 0) and not a continuation
+QF_HD uint64_t bl_run_starts(uint64_t x) { return (x | (x >> 2)) & ~(x >> 1) & BL_LO; }
+
+// ---- descriptor access for the decoupled look-back ----------------------
+// A descriptor is one aligned 64-bit word holding both its flag and its
+// value, and a reader uses nothing else its writer stored, so relaxed
+// gpu-scope accesses suffice (no fence, no L1 invalidation on the reader).
+#ifdef __CUDACC__
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p)
 {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 #endif

@@ -77,7 +77,7 @@ static LayoutPlan plan_layout(uint32_t q, uint32_t r, uint64_t n_expect, uint64_
     uint32_t need = (uint32_t)(avg * 1.05 + 10.0 * std::sqrt(avg) + 256.0);
     p.threads = tb >= 10 ? (1 << (tb - 5)) : 32;
     size_t S = (size_t)1 << tb;
-    size_t tile = (((S + SPILL_SLOTS) * bpe + 32 + 15) & ~(size_t)15) + S / 8;
+    size_t tile = tile_bytes(tb, bpe) + S / 8;
     size_t counters = 4 * (S / 2 + S / 32 + 8);
     size_t bitmaps = 4 * (S + S / 8);
     size_t budget = 100 * 1024;
@@ -470,9 +470,12 @@ static int lookup_unsorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uin
     TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
     if (n > 0) {
         const DeviceInfo &di = device_info(current_device());
-        uint32_t per_block = LOOKUP_THREADS * LOOKUP_QPT;
-        uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)di.sms * 32);
-        k_lookup_unsorted<BPE><<<grid, LOOKUP_THREADS, 0, s>>>(keys, (uint32_t)n, v, out);
+        // one-byte slots: two queries per thread (more threads in flight
+        // beat more loads per thread for the dependent word walks)
+        constexpr int QPT = BPE == 1 ? 2 : LOOKUP_QPT;
+        const uint32_t per_block = LOOKUP_THREADS * QPT;
+        const uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)di.sms * 32);
+        k_lookup_unsorted<BPE, QPT><<<grid, LOOKUP_THREADS, 0, s>>>(keys, (uint32_t)n, v, out);
         count_launches(1);
     }
     return call_end(ar, s, ms);

@@ -248,56 +248,65 @@ __global__ void __launch_bounds__(THREADS) k_bucket_hist(
 }
 
 // ---------------------------------------------------------------------
-// Decoupled look-back over bucket descriptors, one warp: each round reads
-// the 32 nearest unread predecessors at once (lane l holds bucket j - l),
-// waits until all 32 are published, then folds them far-to-near with an
-// ordered shuffle reduction up to the nearest inclusive descriptor.  Returns (on every lane) the slot
-// at which bucket b's items start (c_in).
+// Decoupled look-back over bucket descriptors, one warp.  Each round issues
+// the loads of the LB_WINDOWS x 32 nearest unread predecessors at once
+// (window m, lane l holds bucket j - 32m - l), so a look-back that has to
+// pass a few hundred buckets still costs one memory round trip; windows are
+// then folded nearest first: wait until the window is published, fold its
+// descriptors far-to-near with an ordered shuffle reduction up to the
+// nearest inclusive descriptor.  Returns (on every lane) the slot at which
+// bucket b's items start (c_in).
 // ---------------------------------------------------------------------
+constexpr int LB_WINDOWS = 4;
+
 __device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_t b, uint32_t *err)
 {
     const int lane = threadIdx.x & 31;
     LayoutFn acc{0u, 0u};  // functions of the windows already folded (nearer buckets)
     int j = (int)b - 1;
     for (;;) {
-        int idx = j - lane;
-        unsigned long long v = idx >= 0 ? 0ull : lb_pack_inc(0u);  // before bucket 0: slot 0
-        uint32_t spins = 0;
-        bool timed_out = false;
-        for (;;) {
-            if (idx >= 0 && (v >> 62) == 0) v = ld_acquire_u64(status + idx);
-            unsigned pending = __ballot_sync(0xffffffffu, (v >> 62) == 0);
-            if (!pending) break;
-            if (++spins > SPIN_LIMIT) {
-                timed_out = true;
-                break;
-            }
-            __nanosleep(32);
-        }
-        if (timed_out) {
-            if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
-            return 0u;
-        }
-        unsigned incm = __ballot_sync(0xffffffffu, (v >> 62) == 2ull);
-        const int L = incm ? __ffs(incm) - 1 : 32;  // nearest inclusive lane
-        // lane function: aggregate map; the inclusive lane becomes the
-        // constant max(c, c_L) (applied to c = 0); lanes past it identity
-        LayoutFn f{0u, 0u};
-        if (lane < L) f = LayoutFn{(uint32_t)((v >> 31) & LB_VMAX), (uint32_t)(v & LB_VMAX)};
-        else if (lane == L) f = LayoutFn{0u, (uint32_t)(v & LB_VMAX)};
-        // ordered reduction: farther lanes (higher index) apply first
+        unsigned long long v[LB_WINDOWS];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            LayoutFn far;
-            far.n = __shfl_down_sync(0xffffffffu, f.n, o);
-            far.F = __shfl_down_sync(0xffffffffu, f.F, o);
-            if (lane + o < 32 && (lane & (2 * o - 1)) == 0) f = compose(far, f);
+        for (int m = 0; m < LB_WINDOWS; m++) {
+            const int idx = j - 32 * m - lane;
+            v[m] = idx >= 0 ? ld_relaxed_u64(status + idx) : lb_pack_inc(0u);  // before bucket 0: slot 0
         }
-        f.n = __shfl_sync(0xffffffffu, f.n, 0);
-        f.F = __shfl_sync(0xffffffffu, f.F, 0);
-        if (incm) return acc.apply(f.apply(0u));
-        acc = compose(f, acc);
-        j -= 32;
+#pragma unroll
+        for (int m = 0; m < LB_WINDOWS; m++) {
+            const int idx = j - 32 * m - lane;
+            unsigned long long vm = v[m];
+            uint32_t spins = 0;
+            for (;;) {
+                unsigned pending = __ballot_sync(0xffffffffu, (vm >> 62) == 0);
+                if (!pending) break;
+                if (++spins > SPIN_LIMIT) {
+                    if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+                    return 0u;
+                }
+                __nanosleep(32);
+                if (idx >= 0 && (vm >> 62) == 0) vm = ld_relaxed_u64(status + idx);
+            }
+            unsigned incm = __ballot_sync(0xffffffffu, (vm >> 62) == 2ull);
+            const int L = incm ? __ffs(incm) - 1 : 32;  // nearest inclusive lane
+            // lane function: aggregate map; the inclusive lane becomes the
+            // constant max(c, c_L) (applied to c = 0); lanes past it identity
+            LayoutFn f{0u, 0u};
+            if (lane < L) f = LayoutFn{(uint32_t)((vm >> 31) & LB_VMAX), (uint32_t)(vm & LB_VMAX)};
+            else if (lane == L) f = LayoutFn{0u, (uint32_t)(vm & LB_VMAX)};
+            // ordered reduction: farther lanes (higher index) apply first
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                LayoutFn far;
+                far.n = __shfl_down_sync(0xffffffffu, f.n, o);
+                far.F = __shfl_down_sync(0xffffffffu, f.F, o);
+                if (lane + o < 32 && (lane & (2 * o - 1)) == 0) f = compose(far, f);
+            }
+            f.n = __shfl_sync(0xffffffffu, f.n, 0);
+            f.F = __shfl_sync(0xffffffffu, f.F, 0);
+            if (incm) return acc.apply(f.apply(0u));
+            acc = compose(f, acc);
+        }
+        j -= 32 * LB_WINDOWS;
     }
 }
 
@@ -432,12 +441,19 @@ __host__ __device__ inline size_t layout_region0_bytes(uint32_t tb, uint32_t cap
     size_t bit = 4 * (S + S / 8);
     return bitmap && bit > gen ? bit : gen;
 }
+// The tile buffer's byte offsets are skewed by 16 bytes per 128: threads
+// emitting slots about 32 apart then write distinct shared-memory banks, and
+// 16-byte-aligned offsets stay 16-byte aligned.
+__host__ __device__ inline size_t tile_skew(size_t off) { return off + ((off >> 7) << 4); }
+__host__ __device__ inline size_t tile_bytes(uint32_t tb, int bpe)
+{
+    return (tile_skew((((size_t)1 << tb) + SPILL_SLOTS) * bpe + 32) + 16 + 15) & ~(size_t)15;
+}
 __host__ __device__ inline size_t layout_smem_bytes(uint32_t tb, uint32_t cap_items, int bpe, bool bitmap)
 {
     size_t S = (size_t)1 << tb;
     size_t r0 = (layout_region0_bytes(tb, cap_items, bpe, bitmap) + 15) & ~(size_t)15;
-    size_t tile = (((S + SPILL_SLOTS) * bpe + 32) + 15) & ~(size_t)15;
-    return r0 + tile + S / 8;  // + occupied bit per quotient
+    return r0 + tile_bytes(tb, bpe) + S / 8;  // + occupied bit per quotient
 }
 // Extra shared memory of the in-place update decode: per 32-slot word of
 // the staged slice its run-start mask and the run starts before it, per
@@ -513,7 +529,7 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
         // cannot sort here: flag it (the host falls back) and keep the chain alive
         if (tid == 0) {
             atomicOr(a.err, DEV_ERR_BUCKET_CAP);
-            st_release_u64(a.status + b, lb_pack_inc(x0));
+            st_relaxed_u64(a.status + b, lb_pack_inc(x0));
         }
         return;
     }
@@ -910,12 +926,12 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
         if (lane == 0 && (acc.n > LB_VMAX / 2 || acc.F > LB_VMAX / 2)) atomicOr(a.err, DEV_ERR_FULL);
         uint32_t cin = 0;
         if (b != 0) {
-            if (lane == 0) st_release_u64(a.status + b, lb_pack_agg(acc.n, acc.F));
+            if (lane == 0) st_relaxed_u64(a.status + b, lb_pack_agg(acc.n, acc.F));
             cin = lookback_cin_warp(a.status, b, a.err);
         }
         uint32_t cout = acc.apply(cin);
         if (lane == 0) {
-            st_release_u64(a.status + b, lb_pack_inc(cout));
+            st_relaxed_u64(a.status + b, lb_pack_inc(cout));
             s_cin = cin;
             s_cout = cout;
         }
@@ -934,14 +950,14 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
     const size_t ge = gs + (size_t)bufslots * BPE;  // end of the buffered part
     const size_t gal = gs & ~(size_t)15;            // smem byte 0 <-> table byte gal
     // occupied bits of the bucket's own quotients, one bit per slot x0..x0+S
-    uint32_t *s_occ = reinterpret_cast<uint32_t *>(s_tile + (((size_t)BUF * BPE + 32 + 15) & ~(size_t)15));
-    for (size_t i = tid * 16; i < ge - gal; i += THREADS * 16)
+    uint32_t *s_occ = reinterpret_cast<uint32_t *>(s_tile + tile_bytes(a.tb, BPE));
+    for (size_t i = tid * 16; i < tile_skew(ge - gal); i += THREADS * 16)
         *reinterpret_cast<uint4 *>(s_tile + i) = make_uint4(0, 0, 0, 0);
     for (uint32_t i = tid; i < S / 32; i += THREADS) s_occ[i] = 0;
     __syncthreads();
 
     auto put_elem = [&](uint32_t pos, uint32_t e) {
-        uint8_t *d = (pos - lo < bufslots) ? s_tile + ((size_t)pos * BPE - gal) : a.table + (size_t)pos * BPE;
+        uint8_t *d = (pos - lo < bufslots) ? s_tile + tile_skew((size_t)pos * BPE - gal) : a.table + (size_t)pos * BPE;
         if (BPE == 1) {
             d[0] = (uint8_t)e;
         } else {
@@ -1035,13 +1051,13 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
         size_t b_end = ge & ~(size_t)15;
         if (b_end < h_end) b_end = h_end;
         auto byte_out = [&](size_t g) -> uint8_t {
-            uint8_t v = s_tile[g - gal];
+            uint8_t v = s_tile[tile_skew(g - gal)];
             if ((g % BPE) == BPE - 1) v |= (uint8_t)(occ_at(g) << 2);
             return v;
         };
         for (size_t g = gs + tid; g < h_end; g += THREADS) a.table[g] = byte_out(g);
         for (size_t g = h_end + (size_t)tid * 16; g < b_end; g += (size_t)THREADS * 16) {
-            uint4 v = *reinterpret_cast<const uint4 *>(s_tile + (g - gal));
+            uint4 v = *reinterpret_cast<const uint4 *>(s_tile + tile_skew(g - gal));
             if (BPE == 1) {
                 // 16 slots: spread their 16 occupied bits onto bit 2 of each byte
                 uint32_t bits = 0;

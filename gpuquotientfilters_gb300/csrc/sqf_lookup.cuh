@@ -25,9 +25,13 @@ struct TableView {
     uint32_t nwords_full; // 8-byte words fully inside the table
 };
 
-__device__ __forceinline__ uint64_t ld_word(const TableView &v, uint32_t w)
+QF_HD uint64_t ld_word(const TableView &v, uint32_t w)
 {
+#ifdef __CUDA_ARCH__
     if (w < v.nwords_full) return __ldg(reinterpret_cast<const unsigned long long *>(v.t) + w);
+#else
+    if (w < v.nwords_full) return reinterpret_cast<const unsigned long long *>(v.t)[w];
+#endif
     uint64_t x = 0;
     for (uint32_t k = 0; k < 8; k++) {
         uint32_t i = w * 8 + k;
@@ -36,63 +40,77 @@ __device__ __forceinline__ uint64_t ld_word(const TableView &v, uint32_t w)
     return x;
 }
 
-// One query against a table of 1-byte slots (r = 5); x0 is the 8-slot word
-// holding slot fq (loaded by the caller so several queries' first loads
-// can be in flight together).
-__device__ __forceinline__ uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr, uint64_t x0)
+// One query against a table of 1-byte slots (r <= 5), walking 8-slot words
+// with every test done on all 8 bytes of a word at once (byte-lane SWAR:
+// bit 0 of byte k flags slot k, popcounts count slots, the lowest or highest
+// flagged byte finds one).  The walk is the reference's (findRunStartGPU,
+// quotientFilter.cu:172-196, and the run scan of hashAndLookUp, :320-357):
+//   1. home word of fq: not occupied -> miss;
+//   2. back to the last unshifted slot at or below fq (the cluster start or
+//      any later slot where no run is pending), counting
+//      D = #occupied - #run starts in [that slot, fq);
+//   3. forward: fq's run is the (D+1)-th run start at or after fq;
+//   4. the run's elements in slot order up to the first remainder >= fr:
+//      equal -> its slot, greater or end of run -> miss.
+// x0 = the home word, loaded by the caller so several queries' first loads
+// can be in flight together.
+QF_HD uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr, uint64_t x)
 {
-    uint32_t w = fq >> 3, k = fq & 7u;
-    uint64_t x = x0;
-    Flags8 f = flags8(x);
-    if (!((f.occ >> k) & 1u)) return GQF_NOT_FOUND;
-    uint32_t rs = f.nonempty & ~f.cont;   // run starts
-    uint32_t cs = ~f.shift & 0xFFu;       // walk-back stops (not shifted)
+    constexpr uint64_t OCC = 0x0404040404040404ull;  // occupied bit of every byte
+    const uint32_t w = fq >> 3, k = fq & 7u;
+    const uint32_t half = k < 4 ? (uint32_t)x : (uint32_t)(x >> 32);
+    if (!((half >> (8 * (k & 3u) + 2)) & 1u)) return GQF_NOT_FOUND;
+    const uint64_t below = bytes_below(k);
+    const uint64_t rs = bl_run_starts(x);
+    const uint64_t st = bl_unshifted(x) & bytes_below(k + 1);
     int D;
-    const uint32_t below = (1u << k) - 1u;
-    uint32_t m = cs & (below | (1u << k));
-    if (m) {
-        uint32_t rng = below & ~((1u << highest_bit(m)) - 1u);
-        D = popc32(f.occ & rng) - popc32(rs & rng);
+    if (st) {
+        const uint64_t R = below & ~bytes_below(highest_byte(st));
+        D = popc64(x & OCC & R) - popc64(rs & R);
     } else {
-        D = popc32(f.occ & below) - popc32(rs & below);
+        D = popc64(x & OCC & below) - popc64(rs & below);
         for (int ww = (int)w - 1; ww >= 0; ww--) {
-            Flags8 g = flags8(ld_word(v, (uint32_t)ww));
-            uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
-            if (cs2) {
-                uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
-                D += popc32(g.occ & rng) - popc32(rs2 & rng);
+            const uint64_t y = ld_word(v, (uint32_t)ww);
+            const uint64_t s2 = bl_unshifted(y);
+            const uint64_t o2 = y & OCC, r2 = bl_run_starts(y);
+            if (s2) {
+                const uint64_t R = ~bytes_below(highest_byte(s2));
+                D += popc64(o2 & R) - popc64(r2 & R);
                 break;
             }
-            D += popc32(g.occ) - popc32(rs2);
+            D += popc64(o2) - popc64(r2);
         }
     }
-    // forward: the (D+1)-th run start at or after fq
     const uint32_t nwords = (v.nslots + 7) >> 3;
-    uint32_t rsm = rs & ~below;
+    uint64_t rsm = rs & ~below;
     uint32_t ws = w;
     for (;;) {
-        int c = popc32(rsm);
+        const int c = popc64(rsm);
         if (c > D) break;
         D -= c;
         if (++ws >= nwords) return GQF_NOT_FOUND;
         x = ld_word(v, ws);
-        Flags8 g = flags8(x);
-        rsm = g.nonempty & ~g.cont;
+        rsm = bl_run_starts(x);
     }
-    uint32_t lane = (uint32_t)select_bit(rsm, D);
-    uint32_t s = ws * 8 + lane;
+    // byte b of rsm * BL_LO = number of run starts in bytes [0, b]; the
+    // first byte where it exceeds D holds the (D+1)-th
+    uint32_t j = lowest_byte((((rsm * BL_LO) | BL_HI) - (uint64_t)(D + 1) * BL_LO) & BL_HI);
+    uint32_t ef = j + 1;  // first byte that may end the run
+    const uint64_t frl = (uint64_t)fr * BL_LO;
     for (;;) {
-        uint32_t e = (uint32_t)(x >> (8 * lane)) & 0xFFu;
-        uint32_t rem = e >> 3;
-        if (rem == fr) return s;
-        if (rem > fr) return GQF_NOT_FOUND;
-        s++;
-        if (++lane == 8) {
-            lane = 0;
-            if (++ws >= nwords) return GQF_NOT_FOUND;
-            x = ld_word(v, ws);
+        // bit 7 of byte b: remainder of slot b >= fr
+        const uint64_t ge = ((((x >> 3) & 0x1F1F1F1F1F1F1F1Full) | BL_HI) - frl) & BL_HI;
+        const uint64_t ends = (~x >> 1) & BL_LO & ~bytes_below(ef);  // not a continuation
+        const uint32_t e = ends ? lowest_byte(ends) : 8u;
+        const uint64_t m = ge & bytes_below(e) & ~bytes_below(j);
+        if (m) {
+            const uint32_t b = lowest_byte(m);
+            return (((uint32_t)(x >> (8 * b + 3)) & 0x1Fu) == fr) ? ws * 8 + b : GQF_NOT_FOUND;
         }
-        if (!(((uint32_t)(x >> (8 * lane)) >> 1) & 1u)) return GQF_NOT_FOUND;
+        if (e < 8 || ++ws >= nwords) return GQF_NOT_FOUND;
+        x = ld_word(v, ws);
+        j = 0;
+        ef = 0;
     }
 }
 
@@ -165,29 +183,35 @@ __device__ __forceinline__ void sqf_query_batch(const TableView &v, const uint32
     }
 }
 
-// launchUnsortedLookups: LOOKUP_QPT queries per thread, coalesced keys.
-template <int BPE>
+// launchUnsortedLookups: QPT queries per thread, coalesced keys.
+template <int BPE, int QPT>
 __global__ void __launch_bounds__(LOOKUP_THREADS) k_lookup_unsorted(const uint32_t *__restrict__ keys, uint32_t n,
                                                                    TableView v, uint32_t *__restrict__ out)
 {
     const uint32_t fpmask = (v.q + v.r >= 32) ? 0xFFFFFFFFu : ((1u << (v.q + v.r)) - 1u);
-    const uint32_t per_block = LOOKUP_THREADS * LOOKUP_QPT;
+    const uint32_t qmask = (1u << v.q) - 1u, rmask = (1u << v.r) - 1u;
+    const uint32_t per_block = LOOKUP_THREADS * QPT;
     for (uint64_t b0 = (uint64_t)blockIdx.x * per_block; b0 < n; b0 += (uint64_t)gridDim.x * per_block) {
-        uint32_t fp[LOOKUP_QPT], res[LOOKUP_QPT];
-        bool valid[LOOKUP_QPT];
+        uint32_t fp[QPT];
+        bool valid[QPT];
 #pragma unroll
-        for (int k = 0; k < LOOKUP_QPT; k++) {
-            uint64_t i = b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x;
+        for (int k = 0; k < QPT; k++) {
+            const uint64_t i = b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x;
             valid[k] = i < n;
             fp[k] = valid[k] ? __ldg(keys + i) : 0u;
         }
+        uint64_t x[QPT];
 #pragma unroll
-        for (int k = 0; k < LOOKUP_QPT; k++) fp[k] = aphash32(fp[k]) & fpmask;
-        sqf_query_batch<BPE>(v, fp, valid, res);
+        for (int k = 0; k < QPT; k++) {
+            fp[k] = aphash32(fp[k]) & fpmask;
+            x[k] = (BPE == 1 && valid[k]) ? ld_word(v, ((fp[k] >> v.r) & qmask) >> 3) : 0ull;
+        }
 #pragma unroll
-        for (int k = 0; k < LOOKUP_QPT; k++) {
-            uint64_t i = b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x;
-            if (valid[k]) out[i] = res[k];
+        for (int k = 0; k < QPT; k++) {
+            if (!valid[k]) continue;
+            const uint32_t res = BPE == 1 ? sqf_query_b1(v, (fp[k] >> v.r) & qmask, fp[k] & rmask, x[k])
+                                          : sqf_query<BPE>(v, fp[k]);
+            out[b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x] = res;
         }
     }
 }
