@@ -291,7 +291,22 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
         e = set_smem(kernel, smem);
         if (e == cudaSuccess) kernel<<<p.g.nb, threads, smem, s>>>(a);
     };
-    if (src_table && BPE == 1) {
+    if (src_table && BPE == 1 && op == OP_INSERT) {
+        // in-place insert: merge into the staged old slices
+        const size_t msm = merge_plan(p.g.tb).total;
+        auto gm = [&](auto kernel, int threads) {
+            e = set_smem(kernel, msm);
+            if (e == cudaSuccess) kernel<<<p.g.nb, threads, msm, s>>>(a);
+        };
+        switch (p.g.tb) {
+        case 15: gm(k_bucket_insert_merge<1024>, 1024); break;
+        case 14: gm(k_bucket_insert_merge<512>, 512); break;
+        case 13: gm(k_bucket_insert_merge<256>, 256); break;
+        case 12: gm(k_bucket_insert_merge<128>, 128); break;
+        case 11: gm(k_bucket_insert_merge<64>, 64); break;
+        default: gm(k_bucket_insert_merge<32>, 32); break;
+        }
+    } else if (src_table && BPE == 1) {
         switch (p.g.tb) {
         case 15: go(k_bucket_layout<1024, 32, BPE, true>, 1024); break;
         case 14: go(k_bucket_layout<512, 32, BPE, true>, 512); break;
