@@ -864,13 +864,19 @@ __device__ __forceinline__ void bucket_insert_merge(const LayoutArgs &a, const u
             uint64_t m = ours64(w);
             const uint32_t a0 = w * MERGE_WS;
             n += __popcll(m);
-            for (;;) {
+            // every pass consumes a fingerprint or ends the stretch, and every
+            // inner pass clears at least one bit of mm; the guards only back that up
+            for (uint32_t guard = 0;; guard++) {
+                if (guard > MERGE_ITEMS + 1) {
+                    atomicOr(a.fused_fail, 1u);
+                    break;
+                }
                 // next fingerprint in this stretch, or the stretch end
                 const uint32_t stop = (k < k1 && s_ip[s_ord[k]] < a0 + MERGE_WS) ? s_ip[s_ord[k]] : a0 + MERGE_WS;
                 const uint64_t below = stop - a0 >= 64 ? ~0ull : ((1ull << (stop - a0)) - 1ull);
                 uint64_t mm = m & below;
                 m &= ~below;
-                while (mm) {
+                for (uint32_t g2 = 0; mm && g2 <= 64; g2++) {
                     const uint32_t s = (uint32_t)(__ffsll((long long)mm) - 1);
                     const uint32_t sa = x0 + a0 + s;
                     if (c <= sa) {  // no shift from here to the stop
