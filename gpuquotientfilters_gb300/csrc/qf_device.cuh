@@ -140,6 +140,35 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
 }
 #endif
 
+#ifdef __CUDACC__
+// Runs of quotients below slot x0 still pending at x0 -- the lookup's walk
+// back to the cluster start, for slot x0 -- by one warp: each round the 32
+// lanes read the 32 words in front of the last ones, a ballot finds the
+// nearest word holding an unshifted slot, and a warp sum adds #occupied -
+// #run starts from that slot up to x0.  Words before the table read as
+// empty, which ends the walk.  x0 is a multiple of 8; every lane returns D.
+__device__ inline int pending_runs_warp(const uint8_t *table, uint32_t x0)
+{
+    const int lane = threadIdx.x & 31;
+    if (x0 == 0 || !(__ldg(table + x0) & 1u)) return 0;
+    constexpr uint64_t OCC = 0x0404040404040404ull;
+    const unsigned long long *t64 = reinterpret_cast<const unsigned long long *>(table);
+    int D = 0;
+    for (int wend = (int)(x0 >> 3);; wend -= 32) {
+        const int ww = wend - 1 - lane;
+        const uint64_t y = ww >= 0 ? __ldg(t64 + ww) : 0ull;
+        const uint64_t st = bl_unshifted(y);
+        const unsigned stops = __ballot_sync(0xffffffffu, st != 0);
+        const int nearest = stops ? __ffs(stops) - 1 : 32;
+        uint64_t R = 0;
+        if (lane < nearest) R = ~0ull;
+        else if (lane == nearest) R = ~bytes_below(highest_byte(st));
+        D += (int)__reduce_add_sync(0xffffffffu, (unsigned)(popc64(y & OCC & R) - popc64(bl_run_starts(y) & R)));
+        if (stops) return D;
+    }
+}
+#endif
+
 // Look-back descriptor (64 bits): [63:62] flag, payload below.
 //   AGG: [61:31] n (items), [30:0] F (end slot when entering at slot 0)
 //   INC: [30:0] c_out (first slot after this bucket's items)

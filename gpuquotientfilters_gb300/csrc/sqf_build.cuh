@@ -630,23 +630,10 @@ __device__ __forceinline__ void bucket_insert_merge(const LayoutArgs &a, const u
     const uint32_t lmask = (S << r) - 1u;  // local fingerprint: local quotient << r | remainder
     for (uint32_t i = tid; i < nbn; i += THREADS) s_it[i] = a.B.items[bbase + i] & lmask;
     for (uint32_t w = tid; w < NWIN; w += THREADS) s_wcnt[w] = 0;
-    if (tid == 0) {
-        // runs of quotients below x0 still pending at x0 (the lookup's walk
-        // back to the cluster start, for slot x0)
-        int D = 0;
-        if (x0 > 0 && (__ldg(src + x0) & 1u)) {
-            for (int ww = (int)(x0 >> 3) - 1; ww >= 0; ww--) {
-                const Flags8 g = flags8(__ldg(reinterpret_cast<const unsigned long long *>(src) + ww));
-                const uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
-                if (cs2) {
-                    const uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
-                    D += popc32(g.occ & rng) - popc32(rs2 & rng);
-                    break;
-                }
-                D += popc32(g.occ) - popc32(rs2);
-            }
-        }
-        s_D0 = D;
+    if (wid == 0) {
+        // runs of quotients below x0 still pending at x0
+        const int D = pending_runs_warp(src, x0);
+        if (lane == 0) s_D0 = D;
     }
     __syncthreads();
     // index: run starts and non-empty slots over the slice, occupied
@@ -1115,23 +1102,10 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
             }
             *reinterpret_cast<uint4 *>(s_sl + i) = w4;
         }
-        if (tid == 0) {
-            // runs of quotients below x0 still pending at x0: the lookup's
-            // walk back to the cluster start, for slot x0
-            int D = 0;
-            if (x0 > 0 && (src[x0] & 1u)) {
-                for (int ww = (int)(x0 >> 3) - 1; ww >= 0; ww--) {
-                    const Flags8 g = flags8(__ldg(reinterpret_cast<const unsigned long long *>(src) + ww));
-                    const uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
-                    if (cs2) {
-                        const uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
-                        D += popc32(g.occ & rng) - popc32(rs2 & rng);
-                        break;
-                    }
-                    D += popc32(g.occ) - popc32(rs2);
-                }
-            }
-            s_D0 = D;
+        if (wid == 0) {
+            // runs of quotients below x0 still pending at x0
+            const int D = pending_runs_warp(src, x0);
+            if (lane == 0) s_D0 = D;
         }
         __syncthreads();
         // 32-slot masks: run starts over the slice, occupied over the bucket

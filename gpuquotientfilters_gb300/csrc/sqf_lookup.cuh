@@ -306,24 +306,10 @@ static __global__ void __launch_bounds__(LKS_THREADS) k_lookup_bucketed_s(Bucket
         }
         *reinterpret_cast<uint4 *>(s_tab + i) = w4;
     }
-    if (tid == 0) {
-        // runs of quotients below x0 still pending at x0 (sqf_query_b1's
-        // walk back for slot x0)
-        int D = 0;
-        const Flags8 f0 = flags8(ld_word(v, x0 >> 3));
-        if (f0.shift & 1u) {
-            for (int ww = (int)(x0 >> 3) - 1; ww >= 0; ww--) {
-                const Flags8 g = flags8(ld_word(v, (uint32_t)ww));
-                const uint32_t rs2 = g.nonempty & ~g.cont, cs2 = ~g.shift & 0xFFu;
-                if (cs2) {
-                    const uint32_t rng = 0xFFu & ~((1u << highest_bit(cs2)) - 1u);
-                    D += popc32(g.occ & rng) - popc32(rs2 & rng);
-                    break;
-                }
-                D += popc32(g.occ) - popc32(rs2);
-            }
-        }
-        s_D0 = D;
+    if (wid == 0) {
+        // runs of quotients below x0 still pending at x0
+        const int D = pending_runs_warp(v.t, x0);
+        if (lane == 0) s_D0 = D;
     }
     __syncthreads();
     // index: this thread's words [w0, w1)
