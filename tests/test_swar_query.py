@@ -27,7 +27,8 @@ def driver(tmp_path_factory):
     if not nvcc:
         pytest.skip("nvcc not available")
     exe = str(tmp_path_factory.mktemp("swq") / "swar_query_host")
-    r = subprocess.run([nvcc, "-std=c++17", "-O2", "-o", exe, SRC], capture_output=True, text=True)
+    r = subprocess.run([nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe, SRC],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     return exe
 
