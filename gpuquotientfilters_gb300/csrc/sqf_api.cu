@@ -480,10 +480,28 @@ static int lookup_unsorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uin
     const SqfGeom tg = geom_of(qf);
     Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
+    // one-byte slots and a batch of at least one query per 16 slots: build the
+    // pending-run summary (one byte per 8 slots) first
+    const uint32_t nwords = (tg.nslots + 7) / 8;
+    const bool summary = BPE == 1 && (uint64_t)n * 16 >= tg.nslots;
+    uint8_t *sum = nullptr;
+    if (summary) {
+        sum = static_cast<uint8_t *>(arena_reserve(ar, align_up((size_t)nwords, 256)));
+        if (!sum) return GQF_ERR_NOMEM;
+    }
     int st = call_begin(ar, s, ms != nullptr);
     if (st) return st;
     TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
-    if (n > 0) {
+    if (n > 0 && summary) {
+        const DeviceInfo &di = device_info(current_device());
+        const uint32_t tiles = (nwords + PS_THREADS * PS_WPT - 1) / (PS_THREADS * PS_WPT);
+        k_pending_summary<<<tiles, PS_THREADS, 0, s>>>(v, sum);
+        constexpr int QPT = 2;
+        const uint32_t per_block = LOOKUP_THREADS * QPT;
+        const uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)di.sms * 32);
+        k_lookup_unsorted_sum<QPT><<<grid, LOOKUP_THREADS, 0, s>>>(keys, (uint32_t)n, v, sum, out);
+        count_launches(2);
+    } else if (n > 0) {
         const DeviceInfo &di = device_info(current_device());
         // one-byte slots: two queries per thread (more threads in flight
         // beat more loads per thread for the dependent word walks)

@@ -35,10 +35,23 @@ int main(int argc, char **argv)
     gqf::TableView v{tab.data(), q, r, nslots, (uint32_t)tab.size(), (uint32_t)(tab.size() / 8)};
     const size_t n = fpb.size() / 4;
     const uint32_t *fps = reinterpret_cast<const uint32_t *>(fpb.data());
+    // with SWAR_SUMMARY set, each query gets its home word's pending-run
+    // summary byte (the recurrence the summary kernel scans)
+    const bool use_sum = std::getenv("SWAR_SUMMARY") != nullptr;
+    std::vector<int> P;
+    if (use_sum) {
+        const uint32_t nwords = (nslots + 7) / 8;
+        P.resize(nwords);
+        int p = 0;
+        for (uint32_t w = 0; w < nwords; w++) {
+            P[w] = p < 0 || p > 254 ? 255 : p;
+            p = gqf::pend_apply(gqf::pend_word(gqf::ld_word(v, w)), p);
+        }
+    }
     std::vector<uint32_t> out(n);
     for (size_t i = 0; i < n; i++) {
         const uint32_t fq = (fps[i] >> r) & ((1u << q) - 1u), fr = fps[i] & ((1u << r) - 1u);
-        out[i] = gqf::sqf_query_b1(v, fq, fr, gqf::ld_word(v, fq >> 3));
+        out[i] = gqf::sqf_query_b1(v, fq, fr, gqf::ld_word(v, fq >> 3), use_sum ? P[fq >> 3] : -1);
     }
     FILE *f = std::fopen(argv[6], "wb");
     if (!f) return 4;

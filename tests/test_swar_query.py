@@ -33,12 +33,15 @@ def driver(tmp_path_factory):
     return exe
 
 
-def run_driver(exe, tmp_path, t, q, r, fps):
+def run_driver(exe, tmp_path, t, q, r, fps, summary=False):
     tf, ff, of = tmp_path / "t.bin", tmp_path / "f.bin", tmp_path / "o.bin"
     t.tofile(tf)
     np.ascontiguousarray(fps, np.uint32).tofile(ff)
+    env = dict(os.environ)
+    if summary:
+        env["SWAR_SUMMARY"] = "1"
     p = subprocess.run([exe, str(tf), str(ff), str(q), str(r), str(O.sqf_num_slots(q)), str(of)],
-                       capture_output=True, text=True)
+                       capture_output=True, text=True, env=env)
     assert p.returncode == 0, p.stderr
     return np.fromfile(of, np.uint32)
 
@@ -56,6 +59,9 @@ def test_walk_matches_oracle(driver, tmp_path, q, fill, nodup):
     look = np.concatenate([keys, O.mt_keys(1000 + q, n)])
     want = O.sqf_lookup(t, q, r, look)
     got = run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r))
+    assert np.array_equal(got, want)
+    # the same walk starting from the pending-run summary of the home word
+    got = run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r), summary=True)
     assert np.array_equal(got, want)
     # every fingerprint of the quotient space near the table's start and end
     allq = np.arange(1 << (q + r), dtype=np.uint32)
