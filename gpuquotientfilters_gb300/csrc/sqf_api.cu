@@ -518,6 +518,11 @@ template <int BPE>
 static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint32_t *out, cudaStream_t s, float *ms)
 {
     const SqfGeom tg = geom_of(qf);
+    // Results go to the queries' input positions either way (the reference
+    // sorts them back by index, quotientFilter.cu:304-305).  On one-byte slots
+    // a batch of at least one query per 16 slots is answered faster through
+    // the pending-run summary than by bucketing the queries first.
+    if (BPE == 1 && (uint64_t)n * 16 >= tg.nslots) return lookup_unsorted_t<BPE>(qf, n, keys, out, s, ms);
     LayoutPlan p = plan_layout(tg.q, tg.r, (uint64_t)tg.nslots * 8 / 10, (uint64_t)n, false);
     // query buckets: aim for ~4k queries per bucket, table-aligned
     ScratchReq req{p.g.nb, (size_t)std::max(n, 1), true, false, false, tg.nslots};

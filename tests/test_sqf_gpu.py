@@ -102,6 +102,13 @@ def test_build_and_lookups(gqf, cuda, q, r, alpha, seed, nodup):
     assert np.array_equal(f.lookup(look), want)
     assert np.array_equal(f.lookup(look, sorted_=True), want)
     assert (want[: n // 2] != O.NOT_FOUND).all()
+    # a batch under one query per 16 slots takes the other paths (direct walk,
+    # bucketed queries): same answers
+    m = max(1, O.sqf_num_slots(q) // 32)
+    small = np.concatenate([look[: m // 2], look[-(m - m // 2):]])
+    ws = O.sqf_lookup(t, q, r, small)
+    assert np.array_equal(f.lookup(small), ws)
+    assert np.array_equal(f.lookup(small, sorted_=True), ws)
 
 
 def test_build_reference_arithmetic_count(gqf, cuda):
