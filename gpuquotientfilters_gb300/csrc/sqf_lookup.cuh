@@ -277,12 +277,22 @@ static __global__ void __launch_bounds__(PS_THREADS) k_pending_summary(TableView
         const int P = x0 < v.nslots ? pending_runs_warp(v.t, x0) : 0;
         if (lane == 0) s_pin = P;
     }
-    uint64_t x[PS_WPT];
+    PendFn8 fw[PS_WPT];  // the words' maps, kept for the output pass
+    if (w0 + PS_WPT <= v.nwords_full && (reinterpret_cast<uintptr_t>(v.t) & 15u) == 0) {
+        const uint4 *p4 = reinterpret_cast<const uint4 *>(v.t + 8ull * w0);
 #pragma unroll
-    for (int k = 0; k < PS_WPT; k++) x[k] = w0 + k < nwords ? ld_word(v, w0 + k) : 0ull;
-    PendFn8 f = pend_word(x[0]);
+        for (int k = 0; k < PS_WPT / 2; k++) {
+            const uint4 q4 = __ldg(p4 + k);
+            fw[2 * k] = pend_word((uint64_t)q4.x | ((uint64_t)q4.y << 32));
+            fw[2 * k + 1] = pend_word((uint64_t)q4.z | ((uint64_t)q4.w << 32));
+        }
+    } else {
 #pragma unroll
-    for (int k = 1; k < PS_WPT; k++) f = pend_compose(f, pend_word(x[k]));
+        for (int k = 0; k < PS_WPT; k++) fw[k] = pend_word(w0 + k < nwords ? ld_word(v, w0 + k) : 0ull);
+    }
+    PendFn8 f = fw[0];
+#pragma unroll
+    for (int k = 1; k < PS_WPT; k++) f = pend_compose(f, fw[k]);
     // exclusive scan of the thread maps across the block
     PendFn8 incl = f;
 #pragma unroll
@@ -307,7 +317,7 @@ static __global__ void __launch_bounds__(PS_THREADS) k_pending_summary(TableView
 #pragma unroll
     for (int k = 0; k < PS_WPT; k++) {
         out |= (uint64_t)(P < 0 ? 255u : (P > 254 ? 255u : (uint32_t)P)) << (8 * k);
-        P = pend_apply(pend_word(x[k]), P);
+        P = pend_apply(fw[k], P);
     }
     if (w0 + PS_WPT <= nwords) {
         *reinterpret_cast<uint64_t *>(sum + w0) = out;
