@@ -705,6 +705,13 @@ __device__ __forceinline__ void bucket_insert_merge(const LayoutArgs &a, const u
         }
         return (lo << 5) + (uint32_t)select_bit(s_rs32[lo], R - (int)s_rsp[lo]);
     };
+    // the same from a word at or before the run start's (a run of quotient q
+    // starts at or after slot q): a step or two instead of the binary search
+    auto run_start_from = [&](int R, uint32_t w) -> uint32_t {
+        while (w > 0 && (int)s_rsp[w] > R) w--;
+        while (w + 1 < NW && (int)s_rsp[w + 1] <= R) w++;
+        return (w << 5) + (uint32_t)select_bit(s_rs32[w], R - (int)s_rsp[w]);
+    };
     if (tid == 0) {
         // the bucket's old runs occupy slots [pf, pe); runs past the slice,
         // or a last run that may continue past it, cannot be merged here
@@ -726,7 +733,7 @@ __device__ __forceinline__ void bucket_insert_merge(const LayoutArgs &a, const u
             if (R >= nrs) {
                 s_bad = 1;
             } else {
-                const uint32_t p = run_start(R);
+                const uint32_t p = run_start_from(R, ql >> 5);
                 uint32_t t = p;
                 for (;;) {
                     const uint32_t rem = (uint32_t)s_sl[t] >> 3;
@@ -745,7 +752,7 @@ __device__ __forceinline__ void bucket_insert_merge(const LayoutArgs &a, const u
                 if (t == p) fl |= 2;  // in front of the old head
             }
         } else {
-            ip = R < nrs ? run_start(R) : lastne;
+            ip = R < nrs ? run_start_from(R, ql >> 5) : lastne;
             fl |= 2 | 4;
         }
         if (ip >= L) {
