@@ -353,6 +353,12 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, i
                            float *ms)
 {
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
+    // Results go to the queries' input positions either way.  A batch of at
+    // least one query per 16 slots is answered faster by direct probes (a
+    // lookup is a rank and a select inside one or two blocks) than by grouping
+    // the queries by block first.
+    if ((uint64_t)n * 16 >= (uint64_t)cqf->numBlocks * 64)
+        return gqf_rsqf_lookup_unsorted(cqf, n, d_keys, d_out, stream, ms);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const BucketGeom g = rsqf_geom(cqf->qbits, (uint64_t)n);
     Arena &ar = arena(current_device(), s);

@@ -90,6 +90,9 @@ def test_rsqf_build_and_batches(gqf, cuda, q, alpha, seed):
     want = O.rsqf_lookup(o, q, look)
     assert np.array_equal(f.lookup(look, sorted_=True), want)
     assert np.array_equal(f.lookup(look, sorted_=False), want)
+    # under one query per 16 slots the sorted call groups the queries by block
+    small = look[: max(1, (1 << q) // 32)]
+    assert np.array_equal(f.lookup(small, sorted_=True), O.rsqf_lookup(o, q, small))
 
 
 def test_rsqf_duplicates_and_empty_batch(gqf, cuda):
