@@ -101,12 +101,16 @@ int gqf_sqf_bulk_build(const gqf_sqf *qf, int n, const uint32_t *d_keys,
                        int no_duplicates, void *stream, float *ms);
 
 /* launchUnsortedLookups, quotientFilter.cu:359-381: d_out[i] = slot of
- * key i's remainder, or GQF_NOT_FOUND. */
+ * key i's remainder, or GQF_NOT_FOUND.  A batch of at least one query per 16
+ * slots first scans the table into a per-8-slot summary (stream workspace,
+ * slots / 8 bytes) so no query walks back past its home word. */
 int gqf_sqf_lookup_unsorted(const gqf_sqf *qf, int n, const uint32_t *d_keys,
                             uint32_t *d_out, void *stream, float *ms);
 
 /* launchSortedLookups, quotientFilter.cu:272-318: same results as the
- * unsorted lookup, computed over queries grouped by table region. */
+ * unsorted lookup (input order).  Batches of at least one query per 16 slots
+ * take the unsorted path above; smaller ones group the queries by table
+ * region. */
 int gqf_sqf_lookup_sorted(const gqf_sqf *qf, int n, const uint32_t *d_keys,
                           uint32_t *d_out, void *stream, float *ms);
 
@@ -159,7 +163,9 @@ int gqf_rsqf_free(gqf_rsqf *cqf);
  * fingerprint of the batch, or -1 */
 int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
                     int32_t *d_ret, void *stream, float *ms);
-/* launchLookups, RSQF.cu:411-456 (slot or -1, in input order) */
+/* launchLookups, RSQF.cu:411-456 (slot or -1, in input order).  Batches of
+ * at least one query per 16 slots are probed directly, smaller ones grouped
+ * by block first. */
 int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
                            int32_t *d_out, void *stream, float *ms);
 /* launchUnsortedLookups, RSQF.cu:540-563 */
