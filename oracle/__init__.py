@@ -42,12 +42,35 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_ref(ref: str = "/root/reference") -> bool:
+def reference_dir() -> str:
+    """The reference checkout the recipes read: $GQF_REFERENCE_DIR, else the
+    folder this build was set up with."""
+    return os.environ.get("GQF_REFERENCE_DIR", "/root/reference")
+
+
+def build_ref(ref: str | None = None) -> bool:
     """Compile the reference CPU code into _ref/ if the checkout exists."""
+    ref = ref or reference_dir()
     if not os.path.isdir(ref):
         return False
     env = dict(os.environ, REF=ref)
     subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")], env=env,
+                          stdout=subprocess.DEVNULL)
+    return True
+
+
+def build_ref_gpu(ref: str | None = None) -> bool:
+    """Compile the reference's standard-filter GPU source into
+    _ref/ref_sqf_gpu.cubin (device code only) if the checkout exists."""
+    ref = ref or reference_dir()
+    if not os.path.isdir(ref):
+        return False
+    cubin = os.path.join(REF_DIR, "ref_sqf_gpu.cubin")
+    srcs = [os.path.join(HERE, "build_ref_gpu.sh"), os.path.join(HERE, "ref_gpu_shim", "pre.cuh")]
+    if os.path.exists(cubin) and os.path.getmtime(cubin) >= max(map(os.path.getmtime, srcs)):
+        return True
+    env = dict(os.environ, REF=ref)
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref_gpu.sh")], env=env,
                           stdout=subprocess.DEVNULL)
     return True
 

@@ -2,7 +2,7 @@
 # Compiles the reference's CPU code from its own sources (read in place under
 # the reference checkout) into oracle/_ref/ -- test infrastructure only; never
 # part of the product.  Nothing here runs the reference's build system.
-#   REF   reference checkout (default /root/reference)
+#   REF   reference checkout (default: the checkout this recipe was written for)
 # Outputs:
 #   _ref/libref_sqf_fnv.so   SQF CPU_version as shipped (FNV hash)
 #   _ref/libref_sqf_ap.so    SQF CPU_version with fnv_hash made weak and
