@@ -38,6 +38,8 @@ N_DELETE = 1 << 20
 # N_KEYS keys, from one `ncu --set full` capture: k_hash_bucket 384,808,192 + k_bucket_layout
 # 261,271,808 (k_fixup_occ touches a few KB).
 BUILD_DRAM_BYTES = 384808192 + 261271808
+# ops timed in every step but not counted in `value`
+EXTRA_OPS = ("build_dup",)
 
 
 def peaks():
@@ -50,7 +52,7 @@ def peaks():
 
 def algorithmic_bytes(op: str, n: int, T: int) -> float:
     """Bytes one op must move at minimum (per-op model of the design notes)."""
-    if op == "build":
+    if op in ("build", "build_dup"):
         return 12.0 * n + T       # keys in, one fingerprint permutation, table out
     if op == "lookup_unsorted":
         return 40.0 * n           # key + result + one 32-B table sector
@@ -157,7 +159,11 @@ def run_gpu(args, world, rank, local):
     qf = G.initFilterGPU(q, R)
     stream = torch.cuda.current_stream(dev)
 
+    # Config 2 builds with both Dup and NoDup.  The Dup build is timed in every
+    # step and reported in per_op, but kept out of `value` (the NoDup build
+    # right after it overwrites the table, and the step's ops are counted once).
     ops = [
+        ("build_dup", n_keys, lambda: G.bulkBuildSegmentedLayouts(qf, n_keys, d_keys, False, stream=stream)),
         ("build", n_keys, lambda: G.bulkBuildSegmentedLayouts(qf, n_keys, d_keys, True, stream=stream)),
         ("lookup_unsorted", n_look, lambda: G.launchUnsortedLookups(qf, n_look, d_look, d_out, stream=stream)),
         ("lookup_sorted", n_look, lambda: G.launchSortedLookups(qf, n_look, d_look, d_out2, stream=stream)),
@@ -178,7 +184,8 @@ def run_gpu(args, world, rank, local):
             ev1.record(stream)
             ev1.synchronize()
             ms = ev0.elapsed_time(ev1)
-            tot += ms
+            if name not in EXTRA_OPS:
+                tot += ms
             if record is not None:
                 record.setdefault(name, []).append(ms)
         return tot
@@ -203,7 +210,7 @@ def run_gpu(args, world, rank, local):
     clk = clocks.stop()
     launches = G.lib().gqf_kernel_launches() - launches0
     t_max = max_over_ranks(world, t_dev, dev)
-    ops_per_step = sum(n for _, n, _ in ops)
+    ops_per_step = sum(n for name, n, _ in ops if name not in EXTRA_OPS)
     value = world * ops_per_step * args.steps / (t_max / 1e3) / 1e6
     peak, peak_kind = peaks()
     per_op = {}
@@ -548,67 +555,141 @@ def e2e_step(args, G, torch, dev, stream, c, qf):
 
 
 # -------------------------------------------------------------- CPU baseline
-# The whole step (about 20 s on one core).
+# The whole step (about 15 s on the host: the build, inserts and deletes are
+# sequential, the lookups run on every host thread).
 CPU_SAMPLE = dict(q=Q, n_build=N_KEYS, n_lookup=N_LOOKUP, n_insert=N_INSERT, n_delete=N_DELETE)
-# The reference arm's per-step sample: the same step on a q=24 filter at the
-# same 0.8 fill (every count divided by 4), so K + W steps end in about a
-# minute.
-REF_SAMPLE = dict(q=24, n_build=13421773, n_lookup=N_LOOKUP >> 2, n_insert=N_INSERT >> 2, n_delete=N_DELETE >> 2)
 
 
-def cpu_sample_run(sample=CPU_SAMPLE):
+def _oracle_mixed_lookups(O, keys, n, seed, skip):
+    """The lookup batch of workload.mixed_lookups (the same array), drawn
+    with the oracle's MT19937 so the CPU legs load nothing of the product."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    npos = n // 2
+    pos = keys[:npos] if npos == keys.size else keys[rng.choice(keys.size, npos, replace=False)]
+    neg = O.mt_keys(seed, n - npos, skip=skip)
+    out = np.concatenate([pos, neg]).astype(np.uint32)
+    return out[rng.permutation(n)]
+
+
+def cpu_workload(sample=CPU_SAMPLE):
+    import oracle as O
+    keys = O.mt_keys(SEED, sample["n_build"])
+    look = _oracle_mixed_lookups(O, keys, sample["n_lookup"], SEED, skip=sample["n_build"] + sample["n_insert"])
+    ins = O.mt_keys(SEED, sample["n_insert"], skip=sample["n_build"])
+    return keys, look, ins, keys[: sample["n_delete"]]
+
+
+def cpu_sample_run(sample=CPU_SAMPLE, work=None):
     """The oracle port (the sequential algorithm of the reference's
     CPU_version on the GPU table format and hash) on the workload: build by
     sequential insertItem of n_build keys into an empty q-bit table, then the
     lookups (50% present), inserts of fresh keys and deletes of present keys.
-    Returns (M ops/s, seconds, description)."""
+    Returns (M ops/s, seconds, description, threads, per-op seconds)."""
     import oracle as O
-    from gpuquotientfilters_gb300 import workload as W
     q = sample["q"]
-    keys = O.mt_keys(SEED, sample["n_build"])
-    look = W.mixed_lookups(keys, sample["n_lookup"], SEED, skip=sample["n_build"] + sample["n_insert"])
-    ins = O.mt_keys(SEED, sample["n_insert"], skip=sample["n_build"])
-    dels = keys[: sample["n_delete"]]
+    keys, look, ins, dels = work if work is not None else cpu_workload(sample)
     t = O.sqf_new(q, R)
     threads = max(1, os.cpu_count() or 1)
     parts = np.array_split(look, threads)
+    per = {}
     t0 = time.perf_counter()
     O.sqf_insert(t, q, R, keys)
+    t1 = time.perf_counter()
     # lookups are independent reads of the table: one slice per host thread
     # (the C calls run without the interpreter lock)
     with concurrent.futures.ThreadPoolExecutor(threads) as ex:
         list(ex.map(lambda a: O.sqf_lookup(t, q, R, a), parts))
+    t2 = time.perf_counter()
     O.sqf_insert(t, q, R, ins)
+    t3 = time.perf_counter()
     O.sqf_delete(t, q, R, dels)
-    dt = time.perf_counter() - t0
+    t4 = time.perf_counter()
+    dt = t4 - t0
+    per = {"build": {"s": round(t1 - t0, 3), "cores": 1}, "lookup": {"s": round(t2 - t1, 3), "cores": threads},
+           "insert": {"s": round(t3 - t2, 3), "cores": 1}, "delete": {"s": round(t4 - t3, 3), "cores": 1}}
     nops = sample["n_build"] + sample["n_lookup"] + sample["n_insert"] + sample["n_delete"]
     desc = ("oracle port: insertItem of %d keys into an empty q=%d r=5 table, %d inserts and %d deletes on one "
             "thread (the reference CPU algorithm shifts in order), %d lookups on %d threads"
             % (sample["n_build"], q, sample["n_insert"], sample["n_delete"], sample["n_lookup"], threads))
-    return nops / dt / 1e6, dt, desc, threads
+    return nops / dt / 1e6, dt, desc, threads, per
+
+
+def reference_gpu_kernels(args):
+    """The reference's own standard-filter GPU kernels (quotientFilter.cu,
+    compiled unmodified into oracle/_ref/ref_sqf_gpu.cubin when the reference
+    sources were present at build time) on the same q=26 workload, each op
+    timed with CUDA events around the whole reference entry point as the
+    reference times it (its host-side sorts and scans restated with torch,
+    its round loops' host syncs included).  One warm-up and one timed run;
+    L2 flushed before each op.  None when the cubin is absent."""
+    from oracle import ref_gpu as RG
+    if not RG.available():
+        return None
+    import torch
+    keys, look, ins, dels = [RG.device_keys(a) for a in cpu_workload()]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    res = {}
+    for it in range(2):
+        f = RG.RefFilter(Q, R)
+        for name, n, fn in (
+                ("build", keys.numel(), lambda: RG.bulk_build_segmented_layouts(f, keys, True)),
+                ("lookup_unsorted", look.numel(), lambda: RG.unsorted_lookups(f, look)),
+                ("lookup_sorted", look.numel(), lambda: RG.sorted_lookups(f, look)),
+                ("insert", ins.numel(), lambda: RG.insert(f, ins)),
+                ("delete", dels.numel(), lambda: RG.supercluster_deletes(f, dels))):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record()
+            fn()
+            ev1.record()
+            ev1.synchronize()
+            if it == 1:
+                ms = ev0.elapsed_time(ev1)
+                res[name] = {"n": int(n), "ms": round(ms, 3), "mops": round(n / ms / 1e3, 1)}
+        del f
+    tot_ms = sum(v["ms"] for v in res.values())
+    nops = sum(v["n"] for v in res.values())
+    res["step"] = {"ms": round(tot_ms, 3), "mops": round(nops / tot_ms / 1e3, 1)}
+    res["what"] = ("reference quotientFilter.cu kernels from a cubin; thrust/CUB host steps restated with torch; "
+                   "bulkBuildSegmentedLayouts NoDup, launchUnsortedLookups, launchSortedLookups, insert, "
+                   "superclusterDeletes; keys and results stay on the device (no copies timed)")
+    return res
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's CPU algorithm (the oracle port: the
+    reference's own CPU_version sources are not on the GPU machine, and
+    binaries compiled from them here are x86 while the GPU machine is Arm) on
+    the full q=26 workload, plus the reference's own GPU kernels on the same
+    workload as a second comparator."""
     if rank != 0:
         return None
     import oracle as O
     O.build()
-    sample = REF_SAMPLE
+    work = cpu_workload()
     for _ in range(args.warmup):
-        cpu_sample_run(sample)
-    vals, secs = [], 0.0
+        cpu_sample_run(CPU_SAMPLE, work)
+    vals, secs, per = [], 0.0, None
     for _ in range(args.steps):
-        v, dt, desc, threads = cpu_sample_run(sample)
+        v, dt, desc, threads, per = cpu_sample_run(CPU_SAMPLE, work)
         vals.append(v)
         secs += dt
     value = float(np.mean(vals))
+    try:
+        ref_gpu = reference_gpu_kernels(args)
+    except Exception as e:  # the comparator never decides the arm's line
+        ref_gpu = {"error": repr(e)[:300]}
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "M ops/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "SQF r=5 fill 0.8 (MT19937 seed 2): build + lookups + inserts + deletes; per step "
-                                   "the q=24 sample of the q=26 workload (counts / 4)", "sample": sample},
-            "cpu_baseline": {"value": value, "unit": "M ops/s", "cores": threads, "kind": "port", "sample": desc},
-            "e2e": {"value": value, "unit": "M ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": {"workload": "SQF q=26 r=5 fill 0.8: build 53,687,091 keys NoDup + 2^24 unsorted + 2^24 sorted "
+                                   "lookups (50% positive) + 2^20 inserts + 2^20 deletes",
+                       "q": Q, "r": R, "n_keys": N_KEYS, "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "M ops/s", "cores": threads, "cores_per_op": per,
+                             "kind": "port", "sample": desc + " (the whole q=26 step)"},
+            "e2e": {"value": value, "unit": "M ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu_kernels": ref_gpu}
 
 
 def main():
@@ -636,9 +717,9 @@ def main():
         return
     cpu = None
     if not args.no_cpu_baseline:
-        v, dt, desc, threads = cpu_sample_run()
-        cpu = {"value": v, "unit": "M ops/s", "cores": threads, "kind": "port", "sample": desc,
-               "seconds": round(dt, 2)}
+        v, dt, desc, threads, per = cpu_sample_run()
+        cpu = {"value": v, "unit": "M ops/s", "cores": threads, "cores_per_op": per, "kind": "port",
+               "sample": desc, "seconds": round(dt, 2)}
     out = {
         "metric": METRIC, "value": r["value"], "unit": "M ops/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",

@@ -130,6 +130,7 @@ def _lib():
             "gqf_rsqf_save_file": (i32, [cqfp, C.c_char_p]),
             "gqf_sqf_load_file": (i32, [qfp, C.c_char_p]),
             "gqf_rsqf_load_file": (i32, [cqfp, C.c_char_p]),
+            "gqf_debug_lookback_probe": (i32, [vp, C.c_uint, C.c_uint, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -561,20 +561,31 @@ static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint3
 // device image.  Host code must not use the symbol itself as an address;
 // each device's address comes from cudaGetSymbolAddress on that device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GQF_NOALLOC_SCRATCH_BYTES];
-static void *g_noalloc_base[64];
-static std::mutex g_noalloc_mu;
+// Per device: the array's device address (looked up on the first call, with
+// that device current) and a mutex that serialises the calls on it.
+struct NoallocDev {
+    std::mutex mu;
+    void *base = nullptr;
+};
+static std::mutex g_noalloc_map_mu;
+static std::map<int, NoallocDev> g_noalloc_dev;
 
 template <int BPE>
 static int bulk_build_noalloc_t(const gqf_sqf *qf, uint32_t n, const uint32_t *keys, int nodup, cudaStream_t s)
 {
     const int dev = current_device();
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_base[dev & 63]) {
+    NoallocDev *nd;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_map_mu);
+        nd = &g_noalloc_dev[dev];  // std::map nodes stay put
+    }
+    std::lock_guard<std::mutex> lk(nd->mu);
+    if (!nd->base) {
         void *ptr = nullptr;
         GQF_CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
-        g_noalloc_base[dev & 63] = ptr;
+        nd->base = ptr;
     }
-    char *base = static_cast<char *>(g_noalloc_base[dev & 63]);
+    char *base = static_cast<char *>(nd->base);
     const SqfGeom tg = geom_of(qf);
     const bool bitmap_ok = tg.r == 5 && nodup;
     LayoutPlan p = plan_layout(tg.q, tg.r, n, n, bitmap_ok);
@@ -597,10 +608,21 @@ static int bulk_build_noalloc_t(const gqf_sqf *qf, uint32_t n, const uint32_t *k
     }
     int st = launch_layout<BPE>(p, tg, qf->table, A, B, OP_BUILD, nodup, bitmap_ok, nullptr, sc, err, s);
     if (st) return st;
-    GQF_CK(cudaStreamSynchronize(s));
     uint32_t e = 0;
-    GQF_CK(cudaMemcpy(&e, err, sizeof(e), cudaMemcpyDeviceToHost));
+    GQF_CK(cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s));
+    GQF_CK(cudaStreamSynchronize(s));
     return dev_err_to_status(e);
+}
+
+// One warp per bucket runs the build's look-back over host-given
+// descriptors, with a caller-chosen poll limit (test support).
+__global__ void k_lookback_probe(unsigned long long *status, uint32_t nb, uint32_t spin_limit, uint32_t *cin,
+                                 uint32_t *err)
+{
+    const uint32_t b = blockIdx.x;
+    if (b >= nb) return;
+    const uint32_t c = lookback_cin_warp(status, b, err, spin_limit);
+    if ((threadIdx.x & 31) == 0) cin[b] = c;
 }
 
 }  // namespace gqf
@@ -708,6 +730,34 @@ int gqf_sqf_lookup_sorted(const gqf_sqf *qf, int n, const uint32_t *d_keys, uint
 {
     if (!sqf_ok(qf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
     return BPE_DISPATCH(qf, lookup_sorted_t, qf, n, d_keys, d_out, static_cast<cudaStream_t>(stream), ms);
+}
+
+int gqf_debug_lookback_probe(const unsigned long long *status, unsigned int nb, unsigned int spin_limit,
+                             unsigned int *cin)
+{
+    if (!status || !cin || nb == 0 || nb > (1u << 20) || spin_limit == 0) return GQF_ERR_ARG;
+    unsigned long long *d_status = nullptr;
+    uint32_t *d_cin = nullptr, *d_err = nullptr;
+    int st = GQF_OK;
+    uint32_t e = 0;
+    cudaError_t ce = cudaMalloc(&d_status, sizeof(unsigned long long) * nb);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_cin, sizeof(uint32_t) * nb);
+    if (ce == cudaSuccess) ce = cudaMalloc(&d_err, sizeof(uint32_t));
+    if (ce == cudaSuccess) ce = cudaMemcpy(d_status, status, sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemset(d_err, 0, sizeof(uint32_t));
+    if (ce == cudaSuccess) {
+        count_launches(1);
+        k_lookback_probe<<<nb, 32>>>(d_status, nb, spin_limit, d_cin, d_err);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
+    if (ce == cudaSuccess) ce = cudaMemcpy(cin, d_cin, sizeof(uint32_t) * nb, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&e, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    st = ce == cudaSuccess ? dev_err_to_status(e) : GQF_ERR_CUDA;
+    cudaFree(d_status);
+    cudaFree(d_cin);
+    cudaFree(d_err);
+    return st;
 }
 
 }  // extern "C"

@@ -278,11 +278,15 @@ __global__ void __launch_bounds__(THREADS) k_bucket_hist(
 // then folded nearest first: wait until the window is published, fold its
 // descriptors far-to-near with an ordered shuffle reduction up to the
 // nearest inclusive descriptor.  Returns (on every lane) the slot at which
-// bucket b's items start (c_in).
+// bucket b's items start (c_in).  A window holding an unpublished descriptor
+// is re-read at most spin_limit times, 32 ns apart; past that the warp sets
+// DEV_ERR_TIMEOUT and returns 0, so the kernel ends and the host reports
+// GQF_ERR_TIMEOUT.
 // ---------------------------------------------------------------------
 constexpr int LB_WINDOWS = 4;
 
-__device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_t b, uint32_t *err)
+__device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_t b, uint32_t *err,
+                                             uint32_t spin_limit = SPIN_LIMIT)
 {
     const int lane = threadIdx.x & 31;
     LayoutFn acc{0u, 0u};  // functions of the windows already folded (nearer buckets)
@@ -302,7 +306,7 @@ __device__ inline uint32_t lookback_cin_warp(unsigned long long *status, uint32_
             for (;;) {
                 unsigned pending = __ballot_sync(0xffffffffu, (vm >> 62) == 0);
                 if (!pending) break;
-                if (++spins > SPIN_LIMIT) {
+                if (++spins > spin_limit) {
                     if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
                     return 0u;
                 }

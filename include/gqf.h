@@ -145,15 +145,29 @@ int gqf_sqf_merge(const gqf_sqf *qf1, const gqf_sqf *qf2, int no_duplicates,
  * held until the process exits); requests beyond GQF_NOALLOC_MAX_KEYS keys
  * or GQF_NOALLOC_MAX_Q quotient bits return GQF_ERR_LIMIT.  The first call
  * on a device looks up the array's device address, so make that first call
- * before any stream capture.  Every call shares the one array: calls whose
- * work overlaps on the GPU (different streams, or different host threads)
- * race and corrupt each other's results.  The call waits for its work and
- * returns device-side errors like the timed entry points. */
+ * before any stream capture.  Every call on a device shares that device's
+ * one array.  The library serialises calls from different host threads on
+ * one device, and each call waits for its own work before it returns, so
+ * calls only overlap on the GPU when one returned an error after enqueuing
+ * work; calls whose work overlaps on the GPU race and corrupt each other's
+ * results.  Device-side errors are returned like the timed entry points'. */
 #define GQF_NOALLOC_MAX_KEYS (1u << 20)
 #define GQF_NOALLOC_MAX_Q 22
 #define GQF_NOALLOC_SCRATCH_BYTES (12u << 20)
 int gqf_sqf_bulk_build_noalloc(const gqf_sqf *qf, int n, const uint32_t *d_keys,
                                int no_duplicates, void *stream);
+
+/* Test support, no counterpart in the reference.  Runs the bulk build's
+ * decoupled look-back (one warp per bucket) over nb host-given 64-bit bucket
+ * descriptors -- [63:62] flag (0 unpublished, 1 aggregate, 2 inclusive),
+ * aggregate: [61:31] items n, [30:0] end slot F from slot 0; inclusive:
+ * [30:0] first slot after the bucket -- and stores each bucket's entry slot
+ * in cin[b].  A wait on an unpublished descriptor is polled at most
+ * spin_limit times; if any wait runs out the call returns GQF_ERR_TIMEOUT
+ * (those buckets get cin 0) and the device stays usable.  Allocates, and
+ * synchronises the device. */
+int gqf_debug_lookback_probe(const unsigned long long *status, unsigned int nb, unsigned int spin_limit,
+                             unsigned int *cin);
 
 /* ---------------- rank-and-select quotient filter ----------------------- */
 /* initCQFGPU, RSQF.cu:32-40 (zeroed blocks + one guard block) */

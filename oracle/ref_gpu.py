@@ -169,12 +169,21 @@ class RefFilter:
         return self.buf[: self.T].cpu().numpy()
 
 
-def _u32(a: np.ndarray):
+def device_keys(a):
+    """Keys as a CUDA int32 tensor holding the uint32 bits (host arrays are
+    copied in; CUDA tensors pass through)."""
     import torch
+    if isinstance(a, torch.Tensor):
+        return a.contiguous()
     a = np.ascontiguousarray(a, dtype=np.uint32)
-    if (a == NOT_FOUND).any():
-        raise ValueError("key 0xFFFFFFFF never leaves the reference's insert/delete queue")
     return torch.from_numpy(a.view(np.int32)).cuda()
+
+
+def _u32(a):
+    t = device_keys(a)
+    if bool((t == -1).any()):
+        raise ValueError("key 0xFFFFFFFF never leaves the reference's insert/delete queue")
+    return t
 
 
 def _as_u64(t):
@@ -205,7 +214,7 @@ def _quotienting(f: RefFilter, quotients):
     return rem
 
 
-def bulk_build_segmented_layouts(f: RefFilter, keys: np.ndarray, nodup: bool) -> None:
+def bulk_build_segmented_layouts(f: RefFilter, keys, nodup: bool) -> None:
     """bulkBuildSegmentedLayouts (quotientFilter.cu:1446-1559)."""
     import torch
     d_keys = _u32(keys)
@@ -264,7 +273,7 @@ def _write_filter(f: RefFilter, quot, rem, loc):
     _launch("setOccupiedBits", n, 512, n, f.qf, quot)
 
 
-def bulk_build_sequential_shifts(f: RefFilter, keys: np.ndarray, nodup: bool) -> None:
+def bulk_build_sequential_shifts(f: RefFilter, keys, nodup: bool) -> None:
     """bulkBuildSequentialShifts (quotientFilter.cu:930-1058)."""
     import torch
     d_keys = _u32(keys)
@@ -291,7 +300,7 @@ def bulk_build_sequential_shifts(f: RefFilter, keys: np.ndarray, nodup: bool) ->
     _write_filter(f, quot, rem, loc)
 
 
-def bulk_build_parallel_merging(f: RefFilter, keys: np.ndarray, nodup: bool) -> None:
+def bulk_build_parallel_merging(f: RefFilter, keys, nodup: bool) -> None:
     """bulkBuildParallelMerging (quotientFilter.cu:737-878)."""
     import torch
     d_keys = _u32(keys)
@@ -314,7 +323,7 @@ def bulk_build_parallel_merging(f: RefFilter, keys: np.ndarray, nodup: bool) -> 
     _write_filter(f, quot, rem, loc)
 
 
-def _rounds(f: RefFilter, keys: np.ndarray, locate: str, apply: str, apply_threads: int,
+def _rounds(f: RefFilter, keys, locate: str, apply: str, apply_threads: int,
             with_locations: bool) -> int:
     """The supercluster rounds shared by insert (quotientFilter.cu:533-634)
     and superclusterDeletes (:1202-1297): label superclusters, let every
@@ -332,7 +341,7 @@ def _rounds(f: RefFilter, keys: np.ndarray, locate: str, apply: str, apply_threa
     left = queue.numel()
     while left > 0:
         rounds += 1
-        if rounds > keys.size + 2:
+        if rounds > len(keys) + 2:
             raise RuntimeError("reference rounds did not drain the queue")
         _launch(locate, fs, 1024, fs, f.qf, ind)
         labels = torch.cumsum(ind.to(torch.int64), 0).to(torch.int32).contiguous()
@@ -347,32 +356,40 @@ def _rounds(f: RefFilter, keys: np.ndarray, locate: str, apply: str, apply_threa
     return rounds
 
 
-def insert(f: RefFilter, keys: np.ndarray) -> int:
+def insert(f: RefFilter, keys) -> int:
     """insert (quotientFilter.cu:533-634); returns the number of rounds."""
     return _rounds(f, keys, "locateInsertSuperclusters", "insertItemGPU", 256, True)
 
 
-def supercluster_deletes(f: RefFilter, keys: np.ndarray) -> int:
+def supercluster_deletes(f: RefFilter, keys) -> int:
     """superclusterDeletes (quotientFilter.cu:1202-1297); returns the
     number of rounds."""
     return _rounds(f, keys, "locateDeleteSuperclusters", "deleteItemGPU", 1024, False)
 
 
-def unsorted_lookups(f: RefFilter, keys: np.ndarray) -> np.ndarray:
+def _host(t, keys):
+    """Results as a host uint32 array for host keys, else the CUDA tensor."""
+    import torch
+    if isinstance(keys, torch.Tensor):
+        return t
+    torch.cuda.synchronize()
+    return t.cpu().numpy().view(np.uint32)
+
+
+def unsorted_lookups(f: RefFilter, keys):
     """launchUnsortedLookups (quotientFilter.cu:359-381)."""
     import torch
-    d = torch.from_numpy(np.ascontiguousarray(keys, dtype=np.uint32).view(np.int32)).cuda()
+    d = device_keys(keys)
     out = torch.zeros(d.numel(), dtype=torch.int32, device="cuda")
     _launch("hashAndLookUp", d.numel(), 1024, d.numel(), f.qf, d, out)
-    torch.cuda.synchronize()
-    return out.cpu().numpy().view(np.uint32)
+    return _host(out, keys)
 
 
-def sorted_lookups(f: RefFilter, keys: np.ndarray) -> np.ndarray:
+def sorted_lookups(f: RefFilter, keys):
     """launchSortedLookups (quotientFilter.cu:272-318): hash, sort by hash
     with the input index, look up, sort the results back by index."""
     import torch
-    d = torch.from_numpy(np.ascontiguousarray(keys, dtype=np.uint32).view(np.int32)).cuda()
+    d = device_keys(keys)
     n = d.numel()
     h = torch.zeros(n, dtype=torch.int32, device="cuda")
     _launch("hashInputs", n, 128, n, f.qf, d, h)
@@ -382,5 +399,4 @@ def sorted_lookups(f: RefFilter, keys: np.ndarray) -> np.ndarray:
     _launch("lookUp", n, 1024, n, f.qf, hs, res)
     out = torch.empty_like(res)
     out[order] = res
-    torch.cuda.synchronize()
-    return out.cpu().numpy().view(np.uint32)
+    return _host(out, keys)

@@ -259,6 +259,30 @@ def test_config2_full_size_parity(gqf, cuda):
     assert_same_table(f, t)
 
 
+def test_config2_full_size_dup_parity(gqf, cuda):
+    """q=26, r=5, 53,687,091 keys built with duplicates kept (Dup): every
+    copy of a repeated fingerprint stored, the whole table bit-exact with the
+    oracle; then 2^20 deletes (one copy per occurrence) and a 2^20 insert
+    batch (skipping fingerprints already stored), table exact after each."""
+    from gpuquotientfilters_gb300 import workload as W
+    c = W.config2(n_lookup=1 << 16)
+    q, r = c["q"], c["r"]
+    f = Filter(gqf, cuda, q, r)
+    f.build(c["keys"], False)
+    t = oracle_build(q, r, c["keys"], False)
+    fps = O.aphash(c["keys"], q, r)
+    assert np.unique(fps).size < fps.size  # the build does hold duplicates
+    assert_same_table(f, t)
+    want = O.sqf_lookup(t, q, r, c["lookups"])
+    assert np.array_equal(f.lookup(c["lookups"]), want)
+    f.delete(c["deletes"])
+    O.sqf_delete(t, q, r, c["deletes"])
+    assert_same_table(f, t)
+    f.insert(c["inserts"])
+    O.sqf_insert(t, q, r, c["inserts"])
+    assert_same_table(f, t)
+
+
 def test_skewed_bucket_set_semantics(gqf, cuda):
     """Thousands of fingerprints in one narrow quotient range (one bucket far
     over its average): the set-semantics paths handle any bucket size."""
