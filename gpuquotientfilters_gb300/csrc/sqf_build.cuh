@@ -428,7 +428,13 @@ struct BucketSrc {
     uint32_t stride;
     const uint32_t *cnt;   // nullptr: source absent
     __device__ __forceinline__ size_t start(uint32_t b) const { return base ? (size_t)base[b] : (size_t)b * stride; }
-    __device__ __forceinline__ uint32_t count(uint32_t b) const { return cnt ? cnt[b] : 0u; }
+    // With speculative strides a bucket that overflowed counts more items
+    // than its region holds (the host reruns the op with exact bases); read
+    // at most the region, which keeps the last bucket inside the buffer.
+    __device__ __forceinline__ uint32_t count(uint32_t b) const
+    {
+        return cnt ? (base ? cnt[b] : min(cnt[b], stride)) : 0u;
+    }
 };
 
 struct LayoutArgs {
