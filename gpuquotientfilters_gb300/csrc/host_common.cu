@@ -51,7 +51,10 @@ Arena &arena(int dev, cudaStream_t s)
 {
     std::lock_guard<std::mutex> lk(g_arena_mu);
     std::unique_ptr<Arena> &a = g_arenas[std::make_pair(dev, s)];
-    if (!a) a.reset(new Arena());
+    if (!a) {
+        a.reset(new Arena());
+        a->stream = s;
+    }
     return *a;
 }
 
@@ -66,8 +69,8 @@ int release_arena(int dev, cudaStream_t s)
         a = std::move(it->second);
         g_arenas.erase(it);
     }
+    if (a->ptr) GQF_CK(cudaFreeAsync(a->ptr, s));
     GQF_CK(cudaStreamSynchronize(s));
-    if (a->ptr) GQF_CK(cudaFree(a->ptr));
     if (a->latch) GQF_CK(cudaFree(a->latch));
     if (a->ev0) cudaEventDestroy(a->ev0);
     if (a->ev1) cudaEventDestroy(a->ev1);
@@ -87,14 +90,14 @@ void *arena_reserve(Arena &a, size_t bytes)
     }
     if (bytes <= a.size && a.ptr) return a.ptr;
     if (a.ptr) {
-        // the old buffer may still be in use by queued work
-        cudaDeviceSynchronize();
-        cudaFree(a.ptr);
+        // work queued on the stream may still use the old buffer: free it in
+        // stream order, behind that work
+        cudaFreeAsync(a.ptr, a.stream);
         a.ptr = nullptr;
         a.size = 0;
     }
     size_t want = align_up(bytes < (1u << 20) ? (1u << 20) : bytes, 1u << 20);
-    if (cudaMalloc(&a.ptr, want) != cudaSuccess) {
+    if (cudaMallocAsync(&a.ptr, want, a.stream) != cudaSuccess) {
         a.ptr = nullptr;
         cudaGetLastError();
         return nullptr;

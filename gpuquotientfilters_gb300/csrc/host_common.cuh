@@ -32,10 +32,13 @@ const DeviceInfo &device_info(int dev);
 
 // Grow-only scratch arena, one per (device, stream).  Calls on one stream
 // are serialised by the arena mutex held for the duration of each entry
-// point and run in stream order on the device.
+// point and run in stream order on the device.  The buffer comes from the
+// device's stream-ordered pool on that stream, so growing it frees the old
+// one behind the queued work instead of waiting for the device.
 struct Arena {
     void *ptr = nullptr;
     size_t size = 0;
+    cudaStream_t stream = nullptr;
     uint32_t *latch = nullptr;  // persistent per-device error latch
     uint32_t *err = nullptr;    // per-call device error word
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

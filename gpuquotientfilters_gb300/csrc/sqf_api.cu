@@ -206,17 +206,17 @@ static Scratch carve(void *base, const ScratchReq &r, bool sizing_only, size_t *
 template <int BPE>
 static int extract_into(const uint8_t *table, uint32_t nslots, size_t nbytes, uint32_t r, const BucketGeom &g,
                         Counts3 *tiles, uint32_t *Q, uint32_t *E, uint32_t *base, uint32_t *cnt, uint32_t *dups,
-                        cudaStream_t s)
+                        cudaStream_t s, const uint32_t *gate = nullptr)
 {
     uint32_t ntiles = (nslots + EXTRACT_TILE - 1) / EXTRACT_TILE;
     count_launches(6);
-    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, dups);
-    k_scan_counts3<<<1, 1024, 0, s>>>(tiles, ntiles);
-    k_occ_list<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, Q);
-    k_extract<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, r, tiles, Q, E);
+    k_tile_counts<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, dups, gate);
+    k_scan_counts3<<<1, 1024, 0, s>>>(tiles, ntiles, gate);
+    k_occ_list<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, tiles, Q, gate);
+    k_extract<BPE><<<ntiles, EXTRACT_THREADS, 0, s>>>(table, nslots, (uint32_t)nbytes, r, tiles, Q, E, gate);
     uint32_t grid = (g.nb + 1 + 255) / 256;
-    k_sorted_bounds<<<grid, 256, 0, s>>>(E, &tiles[ntiles].ne, g.nb, g.shift, base, cnt);
-    k_bounds_to_counts<<<grid, 256, 0, s>>>(base, g.nb, cnt);
+    k_sorted_bounds<<<grid, 256, 0, s>>>(E, &tiles[ntiles].ne, g.nb, g.shift, base, cnt, gate);
+    k_bounds_to_counts<<<grid, 256, 0, s>>>(base, g.nb, cnt, gate);
     GQF_CK(cudaGetLastError());
     return GQF_OK;
 }
@@ -256,11 +256,13 @@ static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, S
 template <int BPE>
 static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table, const BucketSrc &A,
                          const BucketSrc &B, int op, int nodup, bool bitmap_ok, const uint32_t *a_dups, Scratch &sc,
-                         uint32_t *err, cudaStream_t s, const uint8_t *src_table = nullptr)
+                         uint32_t *err, cudaStream_t s, const uint8_t *src_table = nullptr,
+                         const uint32_t *gate = nullptr)
 {
     // slots past the last bucket's quotients only receive spill: clear them
+    // (a gated launch leaves that to k_fallback_prepare)
     size_t tail = (size_t)(1u << tg.q) * BPE;
-    if (tg.T > tail) GQF_CK(cudaMemsetAsync(table + tail, 0, tg.T - tail, s));
+    if (!gate && tg.T > tail) GQF_CK(cudaMemsetAsync(table + tail, 0, tg.T - tail, s));
     LayoutArgs a;
     a.A = A;
     a.B = B;
@@ -283,6 +285,7 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
     a.err = err;
     a.src_table = src_table;
     a.fused_fail = src_table ? sc.fused_fail : nullptr;
+    a.gate = gate;
     const size_t smem = p.smem + (src_table ? layout_fused_bytes(p.g.tb) + 16 : 0);
     // one thread per 32 consecutive quotients (fewer per thread below 1024
     // quotients per bucket)
@@ -334,9 +337,30 @@ static int launch_layout(const LayoutPlan &p, const SqfGeom &tg, uint8_t *table,
     GQF_CK(e);
     const DeviceInfo &di = device_info(current_device());
     count_launches(2);
-    k_fixup_occ<BPE><<<di.sms * 2, 256, 0, s>>>(table, sc.fix_list, sc.fix_cnt, sc.fix_cap);
+    k_fixup_occ<BPE><<<di.sms * 2, 256, 0, s>>>(table, sc.fix_list, sc.fix_cnt, sc.fix_cap, gate);
     GQF_CK(cudaGetLastError());
     return GQF_OK;
+}
+
+// Asynchronous in-place update that could not place some bucket (*gate
+// set): reset what the general path's layout expects at zero -- look-back
+// descriptors, bucket ticket, fix-up count, duplicate flag, the call's error
+// word -- and clear the table's spill slots past the last bucket.  The
+// general path then rebuilds every slot from the snapshot's contents.
+__global__ void k_fallback_prepare(const uint32_t *__restrict__ gate, unsigned long long *status, uint32_t nb,
+                                   uint32_t *ticket, uint32_t *fix_cnt, uint32_t *dups, uint32_t *err,
+                                   uint8_t *tail, size_t tail_bytes)
+{
+    if (!*gate) return;
+    const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, step = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = i0; i < nb; i += step) status[i] = 0ull;
+    for (size_t i = i0; i < tail_bytes; i += step) tail[i] = 0;
+    if (i0 == 0) {
+        *ticket = 0;
+        *fix_cnt = 0;
+        *dups = 0;
+        *err = 0;
+    }
 }
 
 enum class Src { NONE, TABLE, KEYS, TABLE2 };
@@ -387,13 +411,19 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
     ScratchReq req_exact = req;
     req_exact.batch_items = std::max<size_t>(n, 1);
     carve(nullptr, req_exact, true, &bytes_exact);
-    // In-place update: a synchronous insert or delete on one-byte slots
-    // with set semantics decodes every bucket's old contents straight from
-    // a snapshot of the table (no extraction pass, see LayoutArgs).  If a
-    // bucket cannot be decoded that way (a table holding duplicate
-    // fingerprints), the table is restored from the snapshot and the op
-    // reruns the general way below.
-    const bool fused = BPE == 1 && bitmap_ok && (op == OP_INSERT || op == OP_DELETE) && ms && !bFromTable;
+    // In-place update: an insert or delete on one-byte slots with set
+    // semantics decodes every bucket's old contents straight from a snapshot
+    // of the table (no extraction pass, see LayoutArgs).  If a bucket cannot
+    // be placed that way (a table holding duplicate fingerprints), the op
+    // reruns the general way from the snapshot: a synchronous call decides
+    // on the host; an asynchronous one queues the general path behind the
+    // in-place kernels with every launch gated on the device-side failure
+    // flag, so it costs only empty launches when the in-place path held.
+    // An insert whose batch averages more than half of MERGE_ITEMS new
+    // fingerprints per bucket would send buckets over the in-place merge's
+    // capacity and end up on the general path anyway: it goes there directly.
+    const bool merge_fits = op != OP_INSERT || (uint64_t)n * 2 <= (uint64_t)p.g.nb * MERGE_ITEMS;
+    const bool fused = BPE == 1 && bitmap_ok && (op == OP_INSERT || op == OP_DELETE) && !bFromTable && merge_fits;
     ScratchReq req_fused = req_exact;
     req_fused.snap_bytes = tg.T;
     size_t bytes_fused = 0;
@@ -403,7 +433,7 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
     float ms_fused = 0.0f;
     if (fused) {
         Scratch sc = carve(base, req_fused, false, &bytes);
-        int st = call_begin(ar, s, true);
+        int st = call_begin(ar, s, ms != nullptr);
         if (st) return st;
         GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
         GQF_CK(cudaMemcpyAsync(sc.snap, qf->table, tg.T, cudaMemcpyDeviceToDevice, s));
@@ -415,6 +445,25 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
         }
         st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, true, nullptr, sc, ar.err, s, sc.snap);
         if (st) return st;
+        if (!ms) {
+            // the general path, gated on the failure flag: contents from the
+            // snapshot, the bucketed batch as it stands
+            const DeviceInfo &di = device_info(current_device());
+            const size_t tail = (size_t)(1u << tg.q) * BPE;
+            count_launches(1);
+            k_fallback_prepare<<<di.sms * 4, 256, 0, s>>>(sc.fused_fail, sc.status, p.g.nb, sc.ticket, sc.fix_cnt,
+                                                           sc.a_dups, ar.err, qf->table + tail,
+                                                           tg.T > tail ? tg.T - tail : 0);
+            GQF_CK(cudaGetLastError());
+            st = extract_into<BPE>(sc.snap, tg.nslots, tg.T, tg.r, p.g, sc.tiles, sc.Q, sc.E, sc.abase, sc.acnt,
+                                   sc.a_dups, s, sc.fused_fail);
+            if (st) return st;
+            A = BucketSrc{sc.E, sc.abase, 0, sc.acnt};
+            st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, bitmap_ok, sc.a_dups, sc, ar.err, s, nullptr,
+                                    sc.fused_fail);
+            if (st) return st;
+            return call_end(ar, s, nullptr);
+        }
         GQF_CK(cudaEventRecord(ar.ev1, s));
         GQF_CK(cudaEventSynchronize(ar.ev1));
         uint32_t e = 0, fail = 0;

@@ -462,6 +462,10 @@ struct LayoutArgs {
     // slice) sets *fused_fail and the host reruns the op the general way.
     const uint8_t *src_table = nullptr;
     uint32_t *fused_fail = nullptr;
+    // When set, the launch does nothing unless *gate is nonzero (the general
+    // path queued behind an asynchronous in-place update, run only if that
+    // update could not place some bucket).
+    const uint32_t *gate = nullptr;
 };
 
 // Shared-memory plan of k_bucket_layout: region 0 holds either the
@@ -1106,6 +1110,7 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
 template <int THREADS, int QPT_, int BPE, bool FUSED = false>
 __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_layout(LayoutArgs a)
 {
+    if (a.gate && !*a.gate) return;
     __shared__ uint32_t s_ticket;
     if (threadIdx.x == 0) s_ticket = atomicAdd(a.ticket, 1u);
     __syncthreads();
@@ -1113,8 +1118,10 @@ __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_bucket_l
 }
 
 template <int BPE>
-__global__ void k_fixup_occ(uint8_t *table, const uint32_t *fix_list, const uint32_t *fix_cnt, uint32_t fix_cap)
+__global__ void k_fixup_occ(uint8_t *table, const uint32_t *fix_list, const uint32_t *fix_cnt, uint32_t fix_cap,
+                            const uint32_t *gate = nullptr)
 {
+    if (gate && !*gate) return;
     uint32_t nf = min(*fix_cnt, fix_cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
         table[(size_t)fix_list[i] * BPE + (BPE - 1)] |= 4u;

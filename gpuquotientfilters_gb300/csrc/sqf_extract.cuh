@@ -105,8 +105,10 @@ struct ThreadSlots {
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_tile_counts(const uint8_t *__restrict__ t, uint32_t nslots,
                                                                 uint32_t nbytes, Counts3 *__restrict__ tiles,
-                                                                uint32_t *__restrict__ dups)
+                                                                uint32_t *__restrict__ dups,
+                                                                const uint32_t *__restrict__ gate = nullptr)
 {
+    if (gate && !*gate) return;
     ThreadSlots<BPE> ts;
     ts.load(t, nslots, nbytes);
     if (dups) {
@@ -154,8 +156,10 @@ __global__ void __launch_bounds__(EXTRACT_THREADS) k_tile_counts(const uint8_t *
 
 // Exclusive scan of the tile counts by one CTA; total written at
 // tiles[ntiles].  Each thread loads its run of tiles with independent loads.
-__global__ void __launch_bounds__(1024) k_scan_counts3(Counts3 *tiles, uint32_t ntiles)
+__global__ void __launch_bounds__(1024) k_scan_counts3(Counts3 *tiles, uint32_t ntiles,
+                                                       const uint32_t *__restrict__ gate = nullptr)
 {
+    if (gate && !*gate) return;
     __shared__ uint32_t sw[3][32];
     const uint32_t per = (ntiles + 1023) / 1024;
     const uint32_t beg = min(ntiles, threadIdx.x * per), end = min(ntiles, beg + per);
@@ -258,8 +262,10 @@ __device__ __forceinline__ void flush_tile(const uint32_t *s_out, uint32_t cnt, 
 template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_occ_list(const uint8_t *__restrict__ t, uint32_t nslots,
                                                              uint32_t nbytes, const Counts3 *__restrict__ tiles,
-                                                             uint32_t *__restrict__ Q)
+                                                             uint32_t *__restrict__ Q,
+                                                             const uint32_t *__restrict__ gate = nullptr)
 {
+    if (gate && !*gate) return;
     __shared__ uint32_t s_out[EXTRACT_TILE];
     ThreadSlots<BPE> ts;
     ts.load(t, nslots, nbytes);
@@ -284,8 +290,10 @@ template <int BPE>
 __global__ void __launch_bounds__(EXTRACT_THREADS) k_extract(const uint8_t *__restrict__ t, uint32_t nslots,
                                                             uint32_t nbytes, uint32_t r,
                                                             const Counts3 *__restrict__ tiles,
-                                                            const uint32_t *__restrict__ Q, uint32_t *__restrict__ E)
+                                                            const uint32_t *__restrict__ Q, uint32_t *__restrict__ E,
+                                                            const uint32_t *__restrict__ gate = nullptr)
 {
+    if (gate && !*gate) return;
     __shared__ uint32_t s_out[EXTRACT_TILE];
     ThreadSlots<BPE> ts;
     ts.load(t, nslots, nbytes);
@@ -310,8 +318,10 @@ __global__ void __launch_bounds__(EXTRACT_THREADS) k_extract(const uint8_t *__re
 
 // Bucket bounds of a sorted fingerprint list: base[b] = lower_bound(b << shift).
 __global__ void k_sorted_bounds(const uint32_t *__restrict__ E, const uint32_t *__restrict__ m_ptr, uint32_t nb,
-                                uint32_t shift, uint32_t *__restrict__ base, uint32_t *__restrict__ cnt)
+                                uint32_t shift, uint32_t *__restrict__ base, uint32_t *__restrict__ cnt,
+                                const uint32_t *__restrict__ gate = nullptr)
 {
+    if (gate && !*gate) return;
     const uint32_t m = *m_ptr;
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= nb; b += gridDim.x * blockDim.x) {
         uint64_t key = (uint64_t)b << shift;
@@ -324,8 +334,10 @@ __global__ void k_sorted_bounds(const uint32_t *__restrict__ E, const uint32_t *
         base[b] = lo;
     }
 }
-__global__ void k_bounds_to_counts(const uint32_t *__restrict__ base, uint32_t nb, uint32_t *__restrict__ cnt)
+__global__ void k_bounds_to_counts(const uint32_t *__restrict__ base, uint32_t nb, uint32_t *__restrict__ cnt,
+                                   const uint32_t *__restrict__ gate = nullptr)
 {
+    if (gate && !*gate) return;
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
         cnt[b] = base[b + 1] - base[b];
 }

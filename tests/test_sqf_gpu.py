@@ -180,6 +180,41 @@ def test_insert_and_delete(gqf, cuda, q, r, alpha, seed, nodup_build):
     assert np.array_equal(f.lookup(look), O.sqf_lookup(t, q, r, look))
 
 
+@pytest.mark.parametrize("q,nodup_build", [(14, True), (16, False), (18, True)])
+def test_insert_and_delete_async(gqf, cuda, q, nodup_build):
+    """Asynchronous inserts and deletes (no ms pointer: only enqueued on a
+    stream) take the in-place path too; on a table holding duplicate
+    fingerprints it cannot place the buckets and the general path queued
+    behind it runs instead, decided on the device.  Tables equal the
+    oracle's either way; the stream's error latch stays clear."""
+    import ctypes as C
+    r = 5
+    n = int(0.8 * (1 << q))
+    keys = O.mt_keys(40 + q, n)
+    if not nodup_build:
+        keys = np.concatenate([keys, keys[: n // 20]])
+    f = Filter(gqf, cuda, q, r)
+    f.build(keys, nodup_build)
+    t = oracle_build(q, r, keys, nodup_build)
+    s = cuda.cuda.Stream()
+    sp = C.c_void_p(s.cuda_stream)
+    L = gqf.lib()
+    # a small insert batch fits the in-place merge; a large one (more new
+    # fingerprints per bucket than it holds) goes to the general path directly
+    for it, frac in enumerate((64, 8)):
+        new = np.concatenate([O.mt_keys(41 + q, max(200, n // frac), skip=n + it * n), keys[:100]])
+        dels = np.concatenate([keys[it * n // 10:(it + 1) * n // 10], new[:200], O.mt_keys(42 + q, 300)])
+        d_new, d_dels = to_dev(cuda, new), to_dev(cuda, dels)
+        cuda.cuda.synchronize()
+        assert L.gqf_sqf_insert(C.byref(f.qf), new.size, d_new.data_ptr(), sp, None) == 0
+        assert L.gqf_sqf_delete(C.byref(f.qf), dels.size, d_dels.data_ptr(), sp, None) == 0
+        s.synchronize()
+        assert L.gqf_stream_status(sp) == 0
+        O.sqf_insert(t, q, r, new)
+        O.sqf_delete(t, q, r, dels)
+        assert_same_table(f, t)
+
+
 def test_insert_into_empty_and_empty_batches(gqf, cuda):
     q, r = 12, 5
     f = Filter(gqf, cuda, q, r)

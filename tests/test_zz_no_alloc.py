@@ -102,7 +102,7 @@ def test_noalloc_build_edge_sizes(gqf, cuda):
     finally:
         G.freeFilterGPU(qf)
     kmax = O.mt_keys(46, 1 << 20)
-    for q, r, nodup, keys in ((22, 5, True, kmax), (22, 5, False, kmax), (19, 13, True, kmax[: int(0.8 * (1 << 19))])):
+    for q, r, nodup, keys in ((22, 5, True, kmax), (22, 5, False, kmax), (18, 13, True, kmax[: int(0.8 * (1 << 18))])):
         qf = G.initFilterGPU(q, r)
         try:
             st = noalloc_build(G, torch, qf, keys, nodup)
