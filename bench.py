@@ -241,53 +241,59 @@ def run_gpu(args, world, rank, local):
 
 
 def rsqf_ops(args, G, torch, dev, stream, flush, peak):
-    """The rank-and-select filter at q=26 (RBITS 5, 64-slot blocks): build to
-    0.9 fill by insertGPU of 60,397,976 MT19937 seed-3 keys into an empty
-    filter, 2^24 sorted lookups (50% positive), then 2^20 incremental
-    inserts.  Reported beside the headline, not counted in it."""
+    """The rank-and-select filter (64-slot blocks): build to 0.9 fill by
+    insertGPU of MT19937 seed-3 keys into an empty filter, 2^24 sorted
+    lookups (50% positive), then 2^20 incremental inserts -- with 5-bit
+    remainders at q=26 (60,397,976 keys), and with 8-bit remainders at q=23,
+    the largest width whose q + 8 fingerprint bits fit the hash's 31
+    (7,549,747 keys).  Reported beside the headline, not counted in it."""
     from gpuquotientfilters_gb300 import workload as W
-    q = args.q
-    n = W.n_keys(q, 0.9, reference_arithmetic=True)
-    n_look, n_ins = N_LOOKUP >> (Q - q), N_INSERT >> (Q - q)
-    keys = G.mt19937(3, n + n_ins)
-    look = W.mixed_lookups(keys[:n], n_look, 3, skip=n + n_ins)
-
-    def dev_u32(a):
-        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
-
-    d_keys, d_ins, d_look = dev_u32(keys[:n]), dev_u32(keys[n:]), dev_u32(look)
-    d_ret = torch.empty(n, dtype=torch.int32, device=dev)
-    d_out = torch.empty(n_look, dtype=torch.int32, device=dev)
-    rec = {}
-    for it in range(args.warmup + args.steps):
-        cqf = G.initCQFGPU(q)
-        torch.cuda.synchronize(dev)
-        for name, fn in (("rsqf_build", lambda: G.insertGPU(cqf, n, d_keys, d_ret, stream=stream)),
-                         ("rsqf_lookup_sorted", lambda: G.launchLookups(cqf, n_look, d_look, d_out, stream=stream)),
-                         ("rsqf_insert", lambda: G.insertGPU(cqf, n_ins, d_ins, d_ret, stream=stream))):
-            flush.fill_(1)
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            fn()
-            ev1.record(stream)
-            ev1.synchronize()
-            if it >= args.warmup:
-                rec.setdefault(name, []).append(ev0.elapsed_time(ev1))
-        G.freeCQFGPU(cqf)
-    nb = G.calcNumBlocksGPU(q)
     out = {}
-    # build: key in, slot out, one fingerprint permutation, blocks written once;
-    # lookup: key, result, two 32-B sectors of a 57-B block; insert: key,
-    # slot, two sectors read and written
-    for name, cnt, nbytes in (("rsqf_build", n, 16.0 * n + 57.0 * (nb + 1)),
-                              ("rsqf_lookup_sorted", n_look, 72.0 * n_look),
-                              ("rsqf_insert", n_ins, 136.0 * n_ins)):
-        ms = float(np.mean(rec[name]))
-        gbs = nbytes / (ms / 1e3) / 1e9
-        out[name] = {"n": cnt, "ms": round(ms, 4), "mops": round(cnt / ms / 1e3, 1), "alg_GBps": round(gbs, 1),
-                     "frac_hbm": round(gbs / peak, 4)}
-    out["workload"] = "RSQF q=%d RBITS 5: insertGPU of %d keys (0.9 fill, MT19937 seed 3) into an empty filter, " \
-                      "%d sorted lookups, %d incremental inserts" % (q, n, n_look, n_ins)
+    for rbits, q, tag in ((5, args.q, "rsqf"), (8, args.q - 3, "rsqf8")):
+        n = W.n_keys(q, 0.9, reference_arithmetic=True)
+        n_look, n_ins = N_LOOKUP >> (Q - args.q), N_INSERT >> (Q - args.q)
+        keys = G.mt19937(3, n + n_ins)
+        look = W.mixed_lookups(keys[:n], n_look, 3, skip=n + n_ins)
+
+        def dev_u32(a):
+            return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).to(dev)
+
+        d_keys, d_ins, d_look = dev_u32(keys[:n]), dev_u32(keys[n:]), dev_u32(look)
+        d_ret = torch.empty(n, dtype=torch.int32, device=dev)
+        d_out = torch.empty(n_look, dtype=torch.int32, device=dev)
+        rec = {}
+        for it in range(args.warmup + args.steps):
+            cqf = G.initCQFGPU(q, rbits)
+            torch.cuda.synchronize(dev)
+            for name, fn in (("build", lambda: G.insertGPU(cqf, n, d_keys, d_ret, stream=stream)),
+                             ("lookup_sorted", lambda: G.launchLookups(cqf, n_look, d_look, d_out, stream=stream)),
+                             ("insert", lambda: G.insertGPU(cqf, n_ins, d_ins, d_ret, stream=stream))):
+                flush.fill_(1)
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                fn()
+                ev1.record(stream)
+                ev1.synchronize()
+                if it >= args.warmup:
+                    rec.setdefault(name, []).append(ev0.elapsed_time(ev1))
+            G.freeCQFGPU(cqf)
+        nb = G.calcNumBlocksGPU(q)
+        bb = 17 + 8 * rbits
+        # build: key in, slot out, one fingerprint permutation, blocks written
+        # once; lookup: key, result, the 32-B sectors of one block (two for
+        # 57 bytes, three for 81); insert: key, slot, those sectors read and
+        # written
+        sect = 64 if rbits == 5 else 96
+        for name, cnt, nbytes in (("build", n, 16.0 * n + bb * (nb + 1.0)),
+                                  ("lookup_sorted", n_look, (8.0 + sect) * n_look),
+                                  ("insert", n_ins, (8.0 + 2 * sect) * n_ins)):
+            ms = float(np.mean(rec[name]))
+            gbs = nbytes / (ms / 1e3) / 1e9
+            out[tag + "_" + name] = {"n": cnt, "ms": round(ms, 4), "mops": round(cnt / ms / 1e3, 1),
+                                     "alg_GBps": round(gbs, 1), "frac_hbm": round(gbs / peak, 4)}
+        out[tag + "_workload"] = ("RSQF q=%d RBITS %d: insertGPU of %d keys (0.9 fill, MT19937 seed 3) into an empty "
+                                  "filter, %d sorted lookups, %d incremental inserts" % (q, rbits, n, n_look, n_ins))
+        del d_keys, d_ins, d_look, d_ret, d_out
     return out
 
 

@@ -106,6 +106,12 @@ def _lib():
             "gqf_rsqf_insert": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_rsqf_lookup_sorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_rsqf_lookup_unsorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_rsqf8_num_blocks": (C.c_size_t, [C.c_uint]),
+            "gqf_rsqf8_init": (i32, [cqfp, C.c_uint]),
+            "gqf_rsqf8_free": (i32, [cqfp]),
+            "gqf_rsqf8_insert": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_rsqf8_lookup_sorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
+            "gqf_rsqf8_lookup_unsorted": (i32, [cqfp, i32, vp, vp, vp, f32p]),
             "gqf_batch_create": (i32, [C.POINTER(C.c_void_p), C.POINTER(gqf_sqf_job), i32, i32,
                                        C.POINTER(gqf_batch_tuning)]),
             "gqf_batch_run": (i32, [C.c_void_p, i32, vp, f32p]),
@@ -320,35 +326,45 @@ def printQuotientFilterGPU(qf) -> None:
 
 
 # ----------------------------------------- rank-and-select quotient filter
-def initCQFGPU(q: int) -> countingQuotientFilterGPU:
+# rbits: the remainder width the reference fixes at compile time (RBITS,
+# RSQF.cuh:21): 5 as shipped, or 8 (the gqf_rsqf8_* entry points).  A
+# filter remembers the width it was made with.
+def _rsqf(cqf, name):
+    return getattr(_lib(), ("gqf_rsqf8_" if getattr(cqf, "_rbits", 5) == 8 else "gqf_rsqf_") + name)
+
+
+def initCQFGPU(q: int, rbits: int = RBITS) -> countingQuotientFilterGPU:
+    if rbits not in (5, 8):
+        raise GQFError(GQF_ERR_ARG, "initCQFGPU: remainder width must be 5 or 8")
     cqf = countingQuotientFilterGPU()
-    _check(_lib().gqf_rsqf_init(C.byref(cqf), q), "initCQFGPU")
+    cqf._rbits = rbits
+    _check(_rsqf(cqf, "init")(C.byref(cqf), q), "initCQFGPU")
     return cqf
 
 
 def freeCQFGPU(cqf) -> None:
-    _check(_lib().gqf_rsqf_free(C.byref(cqf)), "freeCQFGPU")
+    _check(_rsqf(cqf, "free")(C.byref(cqf)), "freeCQFGPU")
 
 
 def insertGPU(cqf, numValues, d_insertValues, d_returnValues, stream=None) -> float:
-    return _timed(_lib().gqf_rsqf_insert, C.byref(cqf), int(numValues), _ptr(d_insertValues),
+    return _timed(_rsqf(cqf, "insert"), C.byref(cqf), int(numValues), _ptr(d_insertValues),
                   _ptr(d_returnValues), stream=stream)
 
 
 def launchLookups(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None) -> float:
-    return _timed(_lib().gqf_rsqf_lookup_sorted, C.byref(cqf), int(numValues), _ptr(d_lookupValues),
+    return _timed(_rsqf(cqf, "lookup_sorted"), C.byref(cqf), int(numValues), _ptr(d_lookupValues),
                   _ptr(d_slotValuesArray), stream=stream)
 
 
 def launchUnsortedLookupsRSQF(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None) -> float:
-    return _timed(_lib().gqf_rsqf_lookup_unsorted, C.byref(cqf), int(numValues), _ptr(d_lookupValues),
+    return _timed(_rsqf(cqf, "lookup_unsorted"), C.byref(cqf), int(numValues), _ptr(d_lookupValues),
                   _ptr(d_slotValuesArray), stream=stream)
 
 
 def rsqf_blocks_bytes(cqf):
     """Host copy of the packed blocks (numpy uint8), guard block included."""
     import numpy as np
-    n = (cqf.numBlocks + 1) * 57
+    n = (cqf.numBlocks + 1) * (17 + 8 * getattr(cqf, "_rbits", 5))
     host = np.empty(n, np.uint8)
     _memcpy_d2h(host.ctypes.data, cqf.blocks, n)
     return host

@@ -40,7 +40,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in sources:
         obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
         objs.append(obj)
-        if force or _stale(obj, [src] + headers):
+        # a translation unit may include another one (rsqf8_api.cu)
+        inc = [os.path.join(CSRC, ln.split('"')[1]) for ln in open(src)
+               if ln.startswith('#include "') and ln.rstrip().endswith('.cu"')]
+        if force or _stale(obj, [src] + inc + headers):
             jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:

@@ -1,9 +1,10 @@
 // Rank-and-select quotient filter (RSQF) device code.
 //
 // Storage is the reference's own packed block layout (RSQF.cuh:24-30):
-// 57 bytes per block = u8 offset, u64 occupieds, u64 runEnds, u64
-// remainders[5] (5-bit fields, slot s at bit 5s, little-endian), so a table
-// written here is byte-identical to the reference's.  One zeroed guard block
+// 17 + 8 * RBITS bytes per block = u8 offset, u64 occupieds, u64 runEnds,
+// u64 remainders[RBITS] (RBITS-bit fields, slot s at bit RBITS * s,
+// little-endian), so a table written here is byte-identical to the
+// reference's.  One zeroed guard block
 // follows the calcNumBlocksGPU() logical blocks: the reference's bounds
 // checks (`blockNum > numBlocks`, RSQF.cu:359,578) let it touch that index.
 //
@@ -24,12 +25,25 @@
 
 #include "qf_device.cuh"
 
-namespace gqf {
+// Remainder width: the reference's RBITS (RSQF.cuh:21, RSQF.h:23), 5 as
+// shipped.  rsqf8_api.cu compiles the same engine with 8, in a namespace and
+// under C names of its own.
+#ifndef GQF_RSQF_R
+#define GQF_RSQF_R 5
+#endif
+#ifndef GQF_RSQF_NS
+#define GQF_RSQF_NS gqf
+#endif
 
-constexpr uint32_t RSQF_BB = 57;   // bytes per packed block
-constexpr uint32_t RSQF_R = 5;     // remainder bits (RSQF.cuh:21)
-constexpr uint32_t RSQF_SPB = 64;  // slots per block (RSQF.cuh:22)
+namespace GQF_RSQF_NS {
+using namespace ::gqf;
+
+constexpr uint32_t RSQF_R = GQF_RSQF_R;                // remainder bits
+constexpr uint32_t RSQF_RMASK = (1u << RSQF_R) - 1u;
+constexpr uint32_t RSQF_BB = 17 + 8 * RSQF_R;          // bytes per packed block: 57 for 5 bits, 81 for 8
+constexpr uint32_t RSQF_SPB = 64;                      // slots per block (RSQF.cuh:22)
 constexpr uint32_t RSQF_NONE = 0xFFFFFFFFu;
+static_assert(RSQF_R == 5 || RSQF_R == 8, "remainder fields of 5 or 8 bits");
 
 __host__ __device__ inline size_t rsqf_table_bytes(uint32_t nblocks)
 {
@@ -101,7 +115,7 @@ struct RsqfView {
     __device__ __forceinline__ uint32_t rem(uint32_t b, uint32_t s) const
     {
         uint32_t bit = s * RSQF_R;
-        return (uint32_t)(ld_u64_unaligned(blk(b) + 17 + (bit >> 3)) >> (bit & 7)) & 31u;
+        return (uint32_t)(ld_u64_unaligned(blk(b) + 17 + (bit >> 3)) >> (bit & 7)) & RSQF_RMASK;
     }
 };
 
@@ -109,7 +123,7 @@ struct RsqfView {
 __device__ inline int32_t rsqf_lookup(const RsqfView &v, uint32_t q, uint32_t fp)
 {
     const uint32_t fq = (fp >> RSQF_R) & ((1u << q) - 1u);
-    const uint32_t fr = fp & 31u;
+    const uint32_t fr = fp & RSQF_RMASK;
     uint32_t b = fq / RSQF_SPB, sl = fq % RSQF_SPB;
     uint64_t occ = v.occ(b);
     if (!((occ >> sl) & 1ull)) return -1;
@@ -219,7 +233,7 @@ struct RsqfGroupTable {
     {
         size_t a = rem_byte(b, s);
         uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);
-        return (w >> ((s * RSQF_R) & 7)) & 31u;
+        return (w >> ((s * RSQF_R) & 7)) & RSQF_RMASK;
     }
     __device__ __forceinline__ void set_byte(size_t a, uint32_t v)
     {
@@ -251,9 +265,9 @@ struct RsqfGroupTable {
         size_t a = rem_byte(b, s);
         uint32_t sh = (s * RSQF_R) & 7;
         uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);  // a field spans at most 2 bytes
-        w = (w & ~(31u << sh)) | ((val & 31u) << sh);
+        w = (w & ~(RSQF_RMASK << sh)) | ((val & RSQF_RMASK) << sh);
         set_byte(a, w & 0xFFu);
-        if (sh > 3) set_byte(a + 1, (w >> 8) & 0xFFu);
+        if (sh + RSQF_R > 8) set_byte(a + 1, (w >> 8) & 0xFFu);
     }
     // The shift loop of the insert (RSQF.cpp:454-476): moves remainders and
     // runEnd bits one slot up from (bn, unused) down to (re_block, end).
@@ -331,7 +345,7 @@ template <typename Tab>
 __device__ inline int32_t rsqf_insert(Tab &f, uint32_t q, uint32_t fp)
 {
     const uint32_t fq = (fp >> RSQF_R) & ((1u << q) - 1u);
-    const uint32_t fr = fp & 31u;
+    const uint32_t fr = fp & RSQF_RMASK;
     const int home = (int)(fq / RSQF_SPB);
     int bn = home;
     const uint32_t hs = fq % RSQF_SPB;
@@ -425,15 +439,16 @@ __device__ inline int32_t rsqf_insert(Tab &f, uint32_t q, uint32_t fp)
 
 // ----------------------------------------------------------------------------
 // Warp-cooperative accessor: one warp replays one group whose blocks are
-// staged in shared memory, 64 bytes per block with aligned fields (+0
-// offset, +8 occupieds, +16 runEnds, +24 remainders[5]).  All 32 lanes run
+// staged in shared memory, 8 * (3 + RBITS) bytes per block with aligned
+// fields (+0 offset, +8 occupieds, +16 runEnds, +24 remainders[RBITS]).  All 32 lanes run
 // the insert redundantly on identical data; lane 0 writes, and the shift
 // loop, the one long loop of an insert into a long cluster, moves runEnd
 // bits and remainder fields a word per lane.  Remainder slots >= 64 keep the
 // reference's flat byte addressing through a map from packed byte offsets
 // to the staged layout.  Blocks right of the group are read from t0.
 // ----------------------------------------------------------------------------
-constexpr uint32_t RSQF_SB = 64;  // staged bytes per block
+constexpr uint32_t RSQF_SW = 3 + RSQF_R;  // staged 8-byte words per block
+constexpr uint32_t RSQF_SB = 8 * RSQF_SW; // staged bytes per block
 
 struct RsqfWarpTable {
     uint8_t *sm;        // staged blocks [glo, ghi)
@@ -484,12 +499,12 @@ struct RsqfWarpTable {
         if (s < RSQF_SPB && in(b)) {
             const uint32_t bit = s * RSQF_R, wi = bit >> 6, sh = bit & 63;
             uint64_t v = w64(b, 24 + 8 * wi) >> sh;
-            if (sh > 59) v |= w64(b, 24 + 8 * (wi + 1)) << (64 - sh);
-            return (uint32_t)v & 31u;
+            if (sh + RSQF_R > 64) v |= w64(b, 24 + 8 * (wi + 1)) << (64 - sh);
+            return (uint32_t)v & RSQF_RMASK;
         }
         const size_t a = (size_t)b * RSQF_BB + 17 + ((size_t)s * RSQF_R >> 3);
         const uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);
-        return (w >> ((s * RSQF_R) & 7)) & 31u;
+        return (w >> ((s * RSQF_R) & 7)) & RSQF_RMASK;
     }
     __device__ __forceinline__ bool wr_ok(uint32_t b)
     {
@@ -528,11 +543,11 @@ struct RsqfWarpTable {
             const uint32_t bit = s * RSQF_R, wi = bit >> 6, sh = bit & 63;
             if (lane == 0) {
                 uint64_t &w = w64(b, 24 + 8 * wi);
-                w = (w & ~(31ull << sh)) | ((uint64_t)(val & 31u) << sh);
-                if (sh > 59) {
+                w = (w & ~((uint64_t)RSQF_RMASK << sh)) | ((uint64_t)(val & RSQF_RMASK) << sh);
+                if (sh + RSQF_R > 64) {
                     uint64_t &w2 = w64(b, 24 + 8 * (wi + 1));
-                    const uint32_t hb = sh + 5 - 64;  // bits in the next word
-                    w2 = (w2 & ~((1ull << hb) - 1)) | ((uint64_t)(val & 31u) >> (5 - hb));
+                    const uint32_t hb = sh + RSQF_R - 64;  // bits in the next word
+                    w2 = (w2 & ~((1ull << hb) - 1)) | ((uint64_t)(val & RSQF_RMASK) >> (RSQF_R - hb));
                 }
             }
             __syncwarp();
@@ -541,9 +556,9 @@ struct RsqfWarpTable {
         const size_t a = (size_t)b * RSQF_BB + 17 + ((size_t)s * RSQF_R >> 3);
         const uint32_t sh = (s * RSQF_R) & 7;
         uint32_t w = byte_at(a) | (byte_at(a + 1) << 8);
-        w = (w & ~(31u << sh)) | ((val & 31u) << sh);
+        w = (w & ~(RSQF_RMASK << sh)) | ((val & RSQF_RMASK) << sh);
         set_byte(a, w & 0xFFu);
-        if (sh > 3) set_byte(a + 1, (w >> 8) & 0xFFu);
+        if (sh + RSQF_R > 8) set_byte(a + 1, (w >> 8) & 0xFFu);
     }
 
     // Moves bits [lo, hi) of a group-wide bit array up by k (k < 64): word u
@@ -575,7 +590,7 @@ struct RsqfWarpTable {
 
     // The insert's shift loop.  Within the group and below slot index 64 (the
     // regular case) it moves the whole range at once: runEnd bits by one
-    // position, remainder fields by five bits; otherwise it runs the
+    // position, remainder fields by RBITS bits; otherwise it runs the
     // reference loop slot by slot.
     __device__ inline bool shift_up(int &bn, uint32_t &unused, int re_block, uint32_t end)
     {
@@ -589,8 +604,8 @@ struct RsqfWarpTable {
         move_bits_up(ga, gb, 1, [base](uint64_t u) {  // runEnds: one word per block
             return reinterpret_cast<uint64_t *>(base + u * RSQF_SB + 16);
         });
-        move_bits_up(ga * RSQF_R, gb * RSQF_R, RSQF_R, [base](uint64_t u) {  // remainders: five words per block
-            return reinterpret_cast<uint64_t *>(base + (u / 5) * RSQF_SB + 24 + (u % 5) * 8);
+        move_bits_up(ga * RSQF_R, gb * RSQF_R, RSQF_R, [base](uint64_t u) {  // remainders: RBITS words per block
+            return reinterpret_cast<uint64_t *>(base + (u / RSQF_R) * RSQF_SB + 24 + (u % RSQF_R) * 8);
         });
         bn = re_block;
         unused = end;
@@ -598,4 +613,4 @@ struct RsqfWarpTable {
     }
 };
 
-}  // namespace gqf
+}  // namespace GQF_RSQF_NS

@@ -1,4 +1,6 @@
 // C ABI of the rank-and-select quotient filter: host orchestration.
+// Compiled twice: as is (RBITS 5, gqf_rsqf_* names) and from rsqf8_api.cu
+// (RBITS 8, gqf_rsqf8_* names).
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -9,7 +11,12 @@
 #include "rsqf_build.cuh"
 #include "sqf_build.cuh"
 
-namespace gqf {
+#ifndef GQF_RSQF_API
+#define GQF_RSQF_API(name) gqf_rsqf_##name
+#endif
+
+namespace GQF_RSQF_NS {
+using namespace ::gqf;
 
 static bool rsqf_q_ok(unsigned q) { return q >= 7 && q + RSQF_R <= 31; }
 
@@ -191,8 +198,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_rsqf_round_warp(
     const uint32_t ng = *count;
     for (uint32_t gi = blockIdx.x * WARPS + wid; gi < ng; gi += gridDim.x * WARPS) {
         const uint32_t b = list[2 * gi], e = list[2 * gi + 1];
-        for (uint32_t i = lane; i < (e - b) * 8; i += 32) {
-            const uint32_t blk = b + i / 8, w = i % 8;
+        for (uint32_t i = lane; i < (e - b) * RSQF_SW; i += 32) {  // staged words: offset, occ, runEnds, remainders
+            const uint32_t blk = b + i / RSQF_SW, w = i % RSQF_SW;
             const uint8_t *src = t0 + (size_t)blk * RSQF_BB;
             uint64_t v;
             if (w == 0) v = src[0];
@@ -267,19 +274,19 @@ __global__ void k_rsqf_merge(uint32_t nblocks, uint8_t *start, uint8_t *active, 
     }
 }
 
-}  // namespace gqf
+}  // namespace GQF_RSQF_NS
 
-using namespace gqf;
+using namespace GQF_RSQF_NS;
 
 extern "C" {
 
-size_t gqf_rsqf_num_blocks(unsigned int q) { return (((size_t)1u << q) + 63) / 64 + 1; }
+size_t GQF_RSQF_API(num_blocks)(unsigned int q) { return (((size_t)1u << q) + 63) / 64 + 1; }
 
-int gqf_rsqf_init(gqf_rsqf *cqf, unsigned int q)
+int GQF_RSQF_API(init)(gqf_rsqf *cqf, unsigned int q)
 {
     if (!cqf || !rsqf_q_ok(q)) return GQF_ERR_ARG;
     cqf->qbits = q;
-    cqf->numBlocks = (unsigned)gqf_rsqf_num_blocks(q);
+    cqf->numBlocks = (unsigned)GQF_RSQF_API(num_blocks)(q);
     size_t bytes = rsqf_table_bytes(cqf->numBlocks);
     void *p = nullptr;
     GQF_CK(cudaMalloc(&p, bytes));
@@ -288,7 +295,7 @@ int gqf_rsqf_init(gqf_rsqf *cqf, unsigned int q)
     return GQF_OK;
 }
 
-int gqf_rsqf_free(gqf_rsqf *cqf)
+int GQF_RSQF_API(free)(gqf_rsqf *cqf)
 {
     if (!cqf) return GQF_ERR_ARG;
     if (cqf->blocks) GQF_CK(cudaFree(cqf->blocks));
@@ -298,10 +305,10 @@ int gqf_rsqf_free(gqf_rsqf *cqf)
 
 static bool rsqf_ok(const gqf_rsqf *c)
 {
-    return c && c->blocks && rsqf_q_ok(c->qbits) && c->numBlocks == gqf_rsqf_num_blocks(c->qbits);
+    return c && c->blocks && rsqf_q_ok(c->qbits) && c->numBlocks == GQF_RSQF_API(num_blocks)(c->qbits);
 }
 
-int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_out, void *stream,
+int GQF_RSQF_API(lookup_unsorted)(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_out, void *stream,
                              float *ms)
 {
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
@@ -349,7 +356,7 @@ static int rsqf_bucket(const uint32_t *keys, uint32_t n, const BucketGeom &g, ui
     return GQF_OK;
 }
 
-int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_out, void *stream,
+int GQF_RSQF_API(lookup_sorted)(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_out, void *stream,
                            float *ms)
 {
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_out))) return GQF_ERR_ARG;
@@ -358,7 +365,7 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, i
     // lookup is a rank and a select inside one or two blocks) than by grouping
     // the queries by block first.
     if ((uint64_t)n * 16 >= (uint64_t)cqf->numBlocks * 64)
-        return gqf_rsqf_lookup_unsorted(cqf, n, d_keys, d_out, stream, ms);
+        return GQF_RSQF_API(lookup_unsorted)(cqf, n, d_keys, d_out, stream, ms);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const BucketGeom g = rsqf_geom(cqf->qbits, (uint64_t)n);
     Arena &ar = arena(current_device(), s);
@@ -424,7 +431,7 @@ static int rsqf_replay_rounds(uint8_t *t, const uint8_t *t0, uint32_t nbl, uint3
     }
 }
 
-int gqf_rsqf_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_ret, void *stream, float *ms)
+int GQF_RSQF_API(insert)(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int32_t *d_ret, void *stream, float *ms)
 {
     if (!rsqf_ok(cqf) || n < 0 || (n > 0 && (!d_keys || !d_ret))) return GQF_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -31,7 +31,7 @@
 
 #include "rsqf.cuh"
 
-namespace gqf {
+namespace GQF_RSQF_NS {
 
 // control words of one insert call (device)
 enum : uint32_t { RCTL_NONEMPTY = 0, RCTL_OVER = 1, RCTL_NSUS = 2, RCTL_WORDS = 4 };
@@ -227,7 +227,9 @@ __global__ void __launch_bounds__(256) k_rsqf_assemble(uint8_t *__restrict__ t, 
         const uint32_t s0 = B * RSQF_SPB;
         const uint32_t a = min(fpos[B], n), e = min(fpos[B + 1], n), c = min(fhome[B], n), d = min(fhome[B + 1], n);
         const uint32_t off = c - a;  // items homed below B stored at or past slot s0
-        uint64_t occ = 0, re = 0, w[5] = {0, 0, 0, 0, 0};
+        uint64_t occ = 0, re = 0, w[RSQF_R];
+#pragma unroll
+        for (int k = 0; k < (int)RSQF_R; k++) w[k] = 0;
         for (uint32_t i = c + lane; i < d; i += 32) occ |= 1ull << ((fps[i] >> RSQF_R) % RSQF_SPB);
         for (uint32_t i = a + lane; i < e; i += 32) {
             const uint32_t fp = fps[i];
@@ -235,11 +237,11 @@ __global__ void __launch_bounds__(256) k_rsqf_assemble(uint8_t *__restrict__ t, 
             const bool last = i + 1 == n || (fps[i + 1] >> RSQF_R) != (fp >> RSQF_R);
             if (last) re |= 1ull << s;
             const uint32_t bit = s * RSQF_R, wi = bit >> 6, sh = bit & 63;
-            const uint64_t r = fp & 31u;
+            const uint64_t r = fp & RSQF_RMASK;
 #pragma unroll
-            for (int k = 0; k < 5; k++) {
+            for (int k = 0; k < (int)RSQF_R; k++) {
                 if ((uint32_t)k == wi) w[k] |= r << sh;
-                if ((uint32_t)k == wi + 1 && sh > 59) w[k] |= r >> (64 - sh);
+                if ((uint32_t)k == wi + 1 && sh + RSQF_R > 64) w[k] |= r >> (64 - sh);
             }
         }
         auto or64 = [](uint64_t x) -> uint64_t {
@@ -250,7 +252,7 @@ __global__ void __launch_bounds__(256) k_rsqf_assemble(uint8_t *__restrict__ t, 
         occ = or64(occ);
         re = or64(re);
 #pragma unroll
-        for (int k = 0; k < 5; k++) w[k] = or64(w[k]);
+        for (int k = 0; k < (int)RSQF_R; k++) w[k] = or64(w[k]);
         uint8_t *blk = t + (size_t)B * RSQF_BB;
         for (uint32_t j = lane; j < RSQF_BB; j += 32) {
             uint8_t v;
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(256) k_rsqf_assemble(uint8_t *__restrict__ t, 
                 const uint32_t k = j - 17;
                 uint64_t x = w[0];
 #pragma unroll
-                for (int q = 1; q < 5; q++)
+                for (int q = 1; q < (int)RSQF_R; q++)
                     if ((k >> 3) == (uint32_t)q) x = w[q];
                 v = (uint8_t)(x >> (8 * (k & 7)));
             }
@@ -474,4 +476,4 @@ __global__ void __launch_bounds__(PEND_THREADS) k_pend_apply(uint32_t nbl, const
     }
 }
 
-}  // namespace gqf
+}  // namespace GQF_RSQF_NS

@@ -186,6 +186,25 @@ int gqf_rsqf_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
 int gqf_rsqf_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
                              int32_t *d_out, void *stream, float *ms);
 
+/* ---------------- rank-and-select filter with 8-bit remainders ---------- */
+/* The same calls for the reference RSQF compiled with RBITS 8 (the
+ * remainder width of RSQF.cuh:21 / RSQF.h:23, a compile-time constant
+ * there): blocks of 81 bytes (u8 offset, u64 occupieds, u64 runEnds, u64
+ * remainders[8]) plus the guard block.  Fingerprints have q + 8 bits, so
+ * q <= 23; a gqf_rsqf handle made by gqf_rsqf8_init is used only with the
+ * gqf_rsqf8_* calls. */
+#define GQF_RSQF8_RBITS 8
+#define GQF_RSQF8_BLOCK_BYTES 81
+size_t gqf_rsqf8_num_blocks(unsigned int q);
+int gqf_rsqf8_init(gqf_rsqf *cqf, unsigned int q);
+int gqf_rsqf8_free(gqf_rsqf *cqf);
+int gqf_rsqf8_insert(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
+                     int32_t *d_ret, void *stream, float *ms);
+int gqf_rsqf8_lookup_sorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
+                            int32_t *d_out, void *stream, float *ms);
+int gqf_rsqf8_lookup_unsorted(const gqf_rsqf *cqf, int n, const uint32_t *d_keys,
+                              int32_t *d_out, void *stream, float *ms);
+
 /* ---------------- batched filters (no counterpart in the reference) ----- */
 /* Many independent standard filters built and queried together: one launch
  * of each pipeline kernel covers every filter of the batch (work lists of

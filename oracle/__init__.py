@@ -233,6 +233,9 @@ class Ref:
         self.fnv = C.CDLL(os.path.join(REF_DIR, "libref_sqf_fnv.so"))
         self.ap = C.CDLL(os.path.join(REF_DIR, "libref_sqf_ap.so"))
         self.rsqf = C.CDLL(os.path.join(REF_DIR, "libref_rsqf.so"))
+        # the same RSQF compiled with RBITS 8, when built
+        p8 = os.path.join(REF_DIR, "libref_rsqf8.so")
+        self.rsqf8 = C.CDLL(p8) if os.path.exists(p8) else None
         for L in (self.fnv, self.ap):
             L.ref_sqf_new.restype = C.c_void_p
             L.ref_sqf_new.argtypes = [C.c_uint, C.c_uint]
@@ -245,22 +248,24 @@ class Ref:
             L.ref_sqf_table.argtypes = [C.c_void_p]
             L.ref_sqf_words.restype = C.c_size_t
             L.ref_sqf_words.argtypes = [C.c_uint, C.c_uint]
-        R = self.rsqf
-        R.ref_rsqf_new.restype = C.c_void_p
-        R.ref_rsqf_new.argtypes = [C.c_uint]
-        R.ref_rsqf_free.argtypes = [C.c_void_p]
-        R.ref_rsqf_insert.restype = C.c_int32
-        R.ref_rsqf_insert.argtypes = [C.c_void_p, C.c_uint32]
-        R.ref_rsqf_lookup.restype = C.c_int32
-        R.ref_rsqf_lookup.argtypes = [C.c_void_p, C.c_uint32]
-        R.ref_rsqf_blocks.restype = C.c_void_p
-        R.ref_rsqf_blocks.argtypes = [C.c_void_p]
-        R.ref_rsqf_block_bytes.restype = C.c_size_t
-        R.ref_rsqf_num_blocks.restype = C.c_size_t
-        R.ref_rsqf_num_blocks.argtypes = [C.c_uint]
-        R.ref_aphash.restype = C.c_uint32
-        R.ref_aphash.argtypes = [C.c_uint32, C.c_uint32]
-        R.ref_mt_fill.argtypes = [C.c_uint32, C.c_uint64, _u32p, C.c_uint64]
+        for R in (self.rsqf, self.rsqf8):
+            if R is None:
+                continue
+            R.ref_rsqf_new.restype = C.c_void_p
+            R.ref_rsqf_new.argtypes = [C.c_uint]
+            R.ref_rsqf_free.argtypes = [C.c_void_p]
+            R.ref_rsqf_insert.restype = C.c_int32
+            R.ref_rsqf_insert.argtypes = [C.c_void_p, C.c_uint32]
+            R.ref_rsqf_lookup.restype = C.c_int32
+            R.ref_rsqf_lookup.argtypes = [C.c_void_p, C.c_uint32]
+            R.ref_rsqf_blocks.restype = C.c_void_p
+            R.ref_rsqf_blocks.argtypes = [C.c_void_p]
+            R.ref_rsqf_block_bytes.restype = C.c_size_t
+            R.ref_rsqf_num_blocks.restype = C.c_size_t
+            R.ref_rsqf_num_blocks.argtypes = [C.c_uint]
+            R.ref_aphash.restype = C.c_uint32
+            R.ref_aphash.argtypes = [C.c_uint32, C.c_uint32]
+            R.ref_mt_fill.argtypes = [C.c_uint32, C.c_uint64, _u32p, C.c_uint64]
 
     @staticmethod
     def available() -> bool:

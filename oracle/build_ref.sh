@@ -8,6 +8,7 @@
 #   _ref/libref_sqf_ap.so    SQF CPU_version with fnv_hash made weak and
 #                            resolved to the reference's Normal_APHash
 #   _ref/libref_rsqf.so      RSQF CPU_version + mt19937ar
+#   _ref/libref_rsqf8.so     the same with RBITS 8
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${REF:-/root/reference}"
@@ -35,5 +36,10 @@ $CXX -shared -o "$OUT/libref_sqf_ap.so" "$OUT/sqf_cpu_weak.o" "$OUT/ref_shim_sqf
 $CXX $FLAGS -c "$REF/mt19937ar.cpp" -o "$OUT/mt.o"
 $CXX $FLAGS -I"$RSQF" -I"$REF" -c "$HERE/ref_shim_rsqf.cpp" -o "$OUT/ref_shim_rsqf.o"
 $CXX -shared -o "$OUT/libref_rsqf.so" "$OUT/rsqf_cpu.o" "$OUT/mt.o" "$OUT/ref_shim_rsqf.o"
+# the same RSQF with 8-bit remainders: RSQF.h's declarations pre-included
+# with RBITS 8 (ref_rsqf8_pre.h), sources unmodified
+$CXX $FLAGS -include "$HERE/ref_rsqf8_pre.h" -c "$RSQF/RSQF.cpp" -o "$OUT/rsqf8_cpu.o"
+$CXX $FLAGS -include "$HERE/ref_rsqf8_pre.h" -I"$RSQF" -I"$REF" -c "$HERE/ref_shim_rsqf.cpp" -o "$OUT/ref_shim_rsqf8.o"
+$CXX -shared -o "$OUT/libref_rsqf8.so" "$OUT/rsqf8_cpu.o" "$OUT/mt.o" "$OUT/ref_shim_rsqf8.o"
 rm -f "$OUT"/*.o
 echo "build_ref: ok -> $OUT"

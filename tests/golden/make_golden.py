@@ -7,7 +7,8 @@ oracle/build_ref.sh (into oracle/_ref/, git-ignored) and records
     sequential insertItem, with its shipped FNV hash and with the GPU's
     Normal_APHash, plus mayContain results for a mixed lookup batch,
   * RSQF CPU_version (RSQF.cpp) packed blocks and return slots after
-    inserting a batch in ascending fingerprint order, plus lookups,
+    inserting a batch in ascending fingerprint order, plus lookups -- as
+    shipped (RBITS 5) and compiled with RBITS 8,
 as SHA-256 digests (and a few raw arrays for small cases), so the oracle
 can be pinned where the reference checkout is absent.
 
@@ -78,36 +79,41 @@ def main():
         sqf_cases.append(case)
     g["sqf_cpu_version"] = sqf_cases
 
-    rsqf_cases = []
-    R = ref.rsqf
-    bb = int(R.ref_rsqf_block_bytes())
-    for (q, n, batch, seed) in [(12, 3686, 256, 3), (14, 14745, 1024, 3), (10, 972, 64, 6)]:
-        k = ref.mt_keys(seed, n)
-        fps = np.array([R.ref_aphash(int(x), 1 << (q + 5)) for x in k], np.uint32)
-        order = np.argsort(fps, kind="stable")
-        f = R.ref_rsqf_new(q)
-        try:
-            rets = np.array([R.ref_rsqf_insert(f, int(x)) for x in k[order]], np.int32)
-            nb = int(R.ref_rsqf_num_blocks(q)) + 1
-            blocks = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)),
-                                           shape=(nb * bb,)).copy()
-            bk = ref.mt_keys(seed, batch, skip=n)
-            bf = np.array([R.ref_aphash(int(x), 1 << (q + 5)) for x in bk], np.uint32)
-            bo = np.argsort(bf, kind="stable")
-            brets = np.array([R.ref_rsqf_insert(f, int(x)) for x in bk[bo]], np.int32)
-            blocks2 = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)),
-                                            shape=(nb * bb,)).copy()
-            look = mixed(k, min(n, 4096), seed, ref)
-            lres = np.array([R.ref_rsqf_lookup(f, int(x)) for x in look], np.int32)
-        finally:
-            R.ref_rsqf_free(f)
-        rsqf_cases.append({
-            "q": q, "n": n, "batch": batch, "seed": seed, "rbits": 5, "block_bytes": bb,
-            "build_blocks_sha256": sha(blocks), "build_rets_sha256": sha(rets),
-            "batch_blocks_sha256": sha(blocks2), "batch_rets_sha256": sha(brets),
-            "lookup_n": int(look.size), "lookup_sha256": sha(lres),
-        })
-    g["rsqf_cpu_version"] = rsqf_cases
+    def rsqf_cases(R, rbits, cases):
+        out = []
+        bb = int(R.ref_rsqf_block_bytes())
+        for (q, n, batch, seed) in cases:
+            k = ref.mt_keys(seed, n)
+            fps = np.array([R.ref_aphash(int(x), 1 << (q + rbits)) for x in k], np.uint32)
+            order = np.argsort(fps, kind="stable")
+            f = R.ref_rsqf_new(q)
+            try:
+                rets = np.array([R.ref_rsqf_insert(f, int(x)) for x in k[order]], np.int32)
+                nb = int(R.ref_rsqf_num_blocks(q)) + 1
+                blocks = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)),
+                                               shape=(nb * bb,)).copy()
+                bk = ref.mt_keys(seed, batch, skip=n)
+                bf = np.array([R.ref_aphash(int(x), 1 << (q + rbits)) for x in bk], np.uint32)
+                bo = np.argsort(bf, kind="stable")
+                brets = np.array([R.ref_rsqf_insert(f, int(x)) for x in bk[bo]], np.int32)
+                blocks2 = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)),
+                                                shape=(nb * bb,)).copy()
+                look = mixed(k, min(n, 4096), seed, ref)
+                lres = np.array([R.ref_rsqf_lookup(f, int(x)) for x in look], np.int32)
+            finally:
+                R.ref_rsqf_free(f)
+            out.append({
+                "q": q, "n": n, "batch": batch, "seed": seed, "rbits": rbits, "block_bytes": bb,
+                "build_blocks_sha256": sha(blocks), "build_rets_sha256": sha(rets),
+                "batch_blocks_sha256": sha(blocks2), "batch_rets_sha256": sha(brets),
+                "lookup_n": int(look.size), "lookup_sha256": sha(lres),
+            })
+        return out
+
+    g["rsqf_cpu_version"] = rsqf_cases(ref.rsqf, 5, [(12, 3686, 256, 3), (14, 14745, 1024, 3), (10, 972, 64, 6)])
+    # RSQF.h with RBITS 8 (oracle/ref_rsqf8_pre.h): 81-byte blocks
+    g["rsqf8_cpu_version"] = rsqf_cases(ref.rsqf8, 8, [(12, 3686, 256, 3), (14, 14745, 1024, 3), (10, 972, 64, 6),
+                                                       (16, 58982, 2048, 7)])
     with open(OUT, "w") as fh:
         json.dump(g, fh, indent=1)
     print("wrote", OUT)

@@ -162,6 +162,25 @@ def test_rsqf_sorted_insert_golden(case):
     assert sha(O.rsqf_lookup(b, q, look)) == case["lookup_sha256"]
 
 
+@pytest.mark.parametrize("case", GOLDEN["rsqf8_cpu_version"], ids=lambda c: "q%d_n%d" % (c["q"], c["n"]))
+def test_rsqf8_sorted_insert_golden(case):
+    """RBITS 8: the oracle against the reference CPU_version compiled with
+    8-bit remainders (81-byte blocks)."""
+    q, n, batch, seed = case["q"], case["n"], case["batch"], case["seed"]
+    assert case["rbits"] == 8 and case["block_bytes"] == 81
+    keys = O.mt_keys(seed, n)
+    b = O.rsqf_new(q, 8)
+    rets = O.rsqf_insert_sorted(b, q, keys, 8)
+    assert sha(b) == case["build_blocks_sha256"]
+    assert sha(rets) == case["build_rets_sha256"]
+    bk = O.mt_keys(seed, batch, skip=n)
+    brets = O.rsqf_insert_sorted(b, q, bk, 8)
+    assert sha(b) == case["batch_blocks_sha256"]
+    assert sha(brets) == case["batch_rets_sha256"]
+    look = mixed(keys, case["lookup_n"], seed)
+    assert sha(O.rsqf_lookup(b, q, look, 8)) == case["lookup_sha256"]
+
+
 @pytest.mark.parametrize("q,alpha,seed", [(10, 0.9, 1), (12, 0.95, 2), (11, 0.5, 3), (12, 0.99, 4)])
 def test_rsqf_sorted_build_is_canonical(q, alpha, seed):
     """Inserting in ascending fingerprint order into an empty RSQF gives the
@@ -266,6 +285,47 @@ def test_rsqf_oracle_vs_reference_sorted_batches(q, alpha, seed):
             rb = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)), shape=(nb * bb,)).copy()
             assert np.array_equal(rr, mr)
             assert np.array_equal(rb, mine)
+    finally:
+        R.ref_rsqf_free(f)
+
+
+@pytest.mark.skipif(not O.Ref.available() or O.Ref().rsqf8 is None,
+                    reason="reference CPU build with RBITS 8 (oracle/_ref) absent")
+@pytest.mark.parametrize("q,alpha,seed,order", [(11, 0.9, 51, "random"), (13, 0.97, 52, "sorted"),
+                                                (16, 0.94, 53, "sorted"), (18, 0.92, 54, "sorted")])
+def test_rsqf8_oracle_vs_reference(q, alpha, seed, order):
+    """RBITS 8: blocks and returns equal the compiled reference's after a
+    build in random or ascending order and two further sorted batches
+    (offset bytes above 64 occur).  Fills stay where the reference stays in
+    its block array: at q=16 and fill 0.96 its insert walks past the array
+    end and places items in the allocation's padding, where the engine
+    (bounded by the guard block) returns -1."""
+    import ctypes as C
+    R = O.Ref().rsqf8
+    n = int(alpha * (1 << q))
+    f = R.ref_rsqf_new(q)
+    mine = O.rsqf_new(q, 8)
+    L = O.lib()
+    try:
+        for k, cnt in enumerate([n, n // 100, n // 100]):
+            keys = O.mt_keys(seed + k, cnt)
+            fps = O.aphash(keys, q, 8)
+            if order == "random" and k == 0:
+                rr = np.array([R.ref_rsqf_insert(f, int(x)) for x in keys], np.int32)
+                mr = np.array([L.or_rsqf_insert_fp(mine, q, 8, int(h)) for h in fps], np.int32)
+            else:
+                o = np.argsort(fps, kind="stable")
+                rr = np.array([R.ref_rsqf_insert(f, int(x)) for x in keys[o]], np.int32)
+                mr = O.rsqf_insert_sorted(mine, q, keys, 8)
+            bb = int(R.ref_rsqf_block_bytes())
+            nb = O.rsqf_num_blocks(q) + 1
+            rb = np.ctypeslib.as_array(C.cast(R.ref_rsqf_blocks(f), C.POINTER(C.c_uint8)), shape=(nb * bb,)).copy()
+            assert bb == 81
+            assert np.array_equal(rr, mr)
+            assert np.array_equal(rb, mine)
+        lk = mixed(O.mt_keys(seed, n), 2000, seed)
+        lr = np.array([R.ref_rsqf_lookup(f, int(x)) for x in lk], np.int32)
+        assert np.array_equal(lr, O.rsqf_lookup(mine, q, lk, 8))
     finally:
         R.ref_rsqf_free(f)
 

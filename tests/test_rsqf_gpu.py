@@ -20,9 +20,9 @@ def sha(a):
 
 
 class RSQF:
-    def __init__(self, G, torch, q):
+    def __init__(self, G, torch, q, rbits=5):
         self.G, self.torch, self.q = G, torch, q
-        self.cqf = G.initCQFGPU(q)
+        self.cqf = G.initCQFGPU(q, rbits)
 
     def __del__(self):
         try:
@@ -45,10 +45,10 @@ class RSQF:
         return self.G.rsqf_blocks_bytes(self.cqf)
 
 
-def assert_same_blocks(g, o):
+def assert_same_blocks(g, o, bb=57):
     if not np.array_equal(g, o):
         d = np.nonzero(g != o)[0]
-        raise AssertionError("%d bytes differ, first at %d (block %d byte %d)" % (d.size, d[0], d[0] // 57, d[0] % 57))
+        raise AssertionError("%d bytes differ, first at %d (block %d byte %d)" % (d.size, d[0], d[0] // bb, d[0] % bb))
 
 
 @pytest.mark.parametrize("case", GOLDEN["rsqf_cpu_version"], ids=lambda c: "q%d_n%d" % (c["q"], c["n"]))
@@ -166,3 +166,51 @@ def test_rsqf_config3_full_size(gqf, cuda):
     assert np.array_equal(ret, want)
     look = W.mixed_lookups(keys[:n], 1 << 22, 3, skip=n + (1 << 20))
     assert np.array_equal(f.lookup(look), O.rsqf_lookup(o, q, look))
+
+
+@pytest.mark.parametrize("case", GOLDEN["rsqf8_cpu_version"], ids=lambda c: "q%d_n%d" % (c["q"], c["n"]))
+def test_rsqf8_golden(gqf, cuda, case):
+    """8-bit remainders (81-byte blocks): the digests of the reference
+    CPU_version compiled with RBITS 8."""
+    q, n, batch, seed = case["q"], case["n"], case["batch"], case["seed"]
+    f = RSQF(gqf, cuda, q, 8)
+    keys = O.mt_keys(seed, n)
+    ret = f.insert(keys)
+    assert sha(f.blocks()) == case["build_blocks_sha256"]
+    assert sha(ret) == case["build_rets_sha256"]
+    bret = f.insert(O.mt_keys(seed, batch, skip=n))
+    assert sha(f.blocks()) == case["batch_blocks_sha256"]
+    assert sha(bret) == case["batch_rets_sha256"]
+    look = np.concatenate([keys[: case["lookup_n"] // 2],
+                           O.mt_keys(seed, case["lookup_n"] - case["lookup_n"] // 2, skip=n)]).astype(np.uint32)
+    assert sha(f.lookup(look)) == case["lookup_sha256"]
+
+
+@pytest.mark.parametrize("q,alpha,seed", [(12, 0.9, 61), (16, 0.94, 62), (20, 0.9, 63), (23, 0.9, 64)])
+def test_rsqf8_build_batches_lookups(gqf, cuda, q, alpha, seed):
+    """8-bit remainders against the oracle: a build into an empty filter,
+    two incremental batches, sorted and unsorted lookups.  q = 23 is the
+    largest width whose q + 8 fingerprint bits fit the 31 the hash uses."""
+    n = int(alpha * (1 << q))
+    keys = O.mt_keys(seed, n)
+    f = RSQF(gqf, cuda, q, 8)
+    o = O.rsqf_new(q, 8)
+    assert np.array_equal(f.insert(keys), O.rsqf_insert_sorted(o, q, keys, 8))
+    assert_same_blocks(f.blocks(), o, 81)
+    for k in range(2):
+        b = O.mt_keys(seed + 10 + k, max(64, n // 64))
+        assert np.array_equal(f.insert(b), O.rsqf_insert_sorted(o, q, b, 8))
+        assert_same_blocks(f.blocks(), o, 81)
+    look = np.concatenate([keys[: n // 2], O.mt_keys(seed + 20, n // 2)])
+    want = O.rsqf_lookup(o, q, look, 8)
+    assert np.array_equal(f.lookup(look, sorted_=True), want)
+    assert np.array_equal(f.lookup(look, sorted_=False), want)
+    small = look[: max(1, (1 << q) // 32)]
+    assert np.array_equal(f.lookup(small, sorted_=True), O.rsqf_lookup(o, q, small, 8))
+
+
+def test_rsqf8_width_limits(gqf, cuda):
+    with pytest.raises(gqf.GQFError):
+        gqf.initCQFGPU(24, 8)  # q + 8 > 31
+    with pytest.raises(gqf.GQFError):
+        gqf.initCQFGPU(12, 6)
