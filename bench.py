@@ -246,12 +246,14 @@ def rsqf_ops(args, G, torch, dev, stream, flush, peak):
     lookups (50% positive), then 2^20 incremental inserts -- with 5-bit
     remainders at q=26 (60,397,976 keys), and with 8-bit remainders at q=23,
     the largest width whose q + 8 fingerprint bits fit the hash's 31
-    (7,549,747 keys).  Reported beside the headline, not counted in it."""
+    (7,549,747 keys, batches scaled to 2^21 lookups and 2^17 inserts so the
+    filter stays within its slots).  Reported beside the headline, not
+    counted in it."""
     from gpuquotientfilters_gb300 import workload as W
     out = {}
     for rbits, q, tag in ((5, args.q, "rsqf"), (8, args.q - 3, "rsqf8")):
         n = W.n_keys(q, 0.9, reference_arithmetic=True)
-        n_look, n_ins = N_LOOKUP >> (Q - args.q), N_INSERT >> (Q - args.q)
+        n_look, n_ins = N_LOOKUP >> (Q - q), N_INSERT >> (Q - q)  # the batches scale with the filter
         keys = G.mt19937(3, n + n_ins)
         look = W.mixed_lookups(keys[:n], n_look, 3, skip=n + n_ins)
 
