@@ -185,12 +185,29 @@ __global__ void k_rsqf_groups(uint32_t nblocks, const uint8_t *__restrict__ star
 // insert its items (fhome: first sorted index homed at or past each block)
 // in ascending order, write the blocks back unless a write left the group
 // (then the group is marked crossed and t is left as it was).
+// Where a build's replay of group [b, e) (items [i0, i1)) may start.  An
+// ascending insert departs from the canonical positions only once its walk
+// meets a block whose offset exceeds 62, and in a cluster that first happens
+// for the first item positioned in the cluster's first such block S1
+// (items before it sit below S1, items homed before the group stay out of
+// it): items [i0, fpos[S1]) are canonical (the rule is pinned on the oracle
+// by tests/test_oracle.py), so the replay writes their canonical state and
+// runs the reference insert from fpos[S1] on.  `sus` marks blocks whose
+// canonical offset exceeds 62; a group without one replays all its items.
+__device__ __forceinline__ uint32_t rsqf_replay_start(const uint8_t *sus, const uint32_t *fpos, uint32_t b,
+                                                      uint32_t e, uint32_t i0, uint32_t i1)
+{
+    for (uint32_t blk = b; blk < e; blk++)
+        if (sus[blk]) return min(max(fpos[blk], i0), i1);
+    return i0;
+}
+
 template <uint32_t MAXB, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_rsqf_round_warp(
     uint8_t *__restrict__ t, const uint8_t *__restrict__ t0, uint32_t nblocks, uint32_t q,
     const uint32_t *__restrict__ fps, const uint32_t *__restrict__ fhome, const uint32_t *__restrict__ list,
     const uint32_t *__restrict__ count, uint8_t *__restrict__ crossed, uint32_t *n_crossed,
-    int32_t *__restrict__ ret, int t0_zero)
+    int32_t *__restrict__ ret, int t0_zero, const uint8_t *__restrict__ sus, const uint32_t *__restrict__ fpos)
 {
     __shared__ __align__(16) uint8_t sm_all[WARPS][MAXB * RSQF_SB];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -211,7 +228,31 @@ __global__ void __launch_bounds__(32 * WARPS) k_rsqf_round_warp(
         __syncwarp();
         RsqfWarpTable f{sm, t0, nblocks, b, e, false, lane, t0_zero != 0};
         const uint32_t i0 = fhome[min(b, nblocks)], i1 = fhome[min(e, nblocks)];
-        for (uint32_t i = i0; i < i1; i++) {
+        uint32_t istart = i0;
+        if (sus) {
+            // a build: the canonical state of the items before the first
+            // block of offset > 62, then the exact replay from there
+            istart = rsqf_replay_start(sus, fpos, b, min(e, nblocks), i0, i1);
+            for (uint32_t i = i0 + lane; i < istart; i += 32) {
+                const uint32_t fp = fps[i], s = (uint32_t)ret[i];
+                const uint32_t blk = s / RSQF_SPB, sl = s % RSQF_SPB, hb = (fp >> RSQF_R) / RSQF_SPB;
+                unsigned long long *bs = reinterpret_cast<unsigned long long *>(sm + (size_t)(blk - b) * RSQF_SB);
+                unsigned long long *bh = reinterpret_cast<unsigned long long *>(sm + (size_t)(hb - b) * RSQF_SB);
+                atomicOr(bh + 1, 1ull << ((fp >> RSQF_R) % RSQF_SPB));  // occupieds of the home block
+                if (i + 1 == istart || (fps[i + 1] >> RSQF_R) != (fp >> RSQF_R)) atomicOr(bs + 2, 1ull << sl);
+                const uint32_t bit = sl * RSQF_R, wi = bit >> 6, sh = bit & 63;
+                const unsigned long long r = fp & RSQF_RMASK;
+                atomicOr(bs + 3 + wi, r << sh);
+                if (sh + RSQF_R > 64) atomicOr(bs + 4 + wi, r >> (64 - sh));
+            }
+            // offsets: items homed below the block and stored in it
+            for (uint32_t blk = b + lane; blk < e && blk < nblocks; blk += 32) {
+                const uint32_t hi = min(fhome[blk], istart), lo = max(fpos[blk], i0);
+                sm[(size_t)(blk - b) * RSQF_SB] = (uint8_t)(hi > lo ? hi - lo : 0u);
+            }
+            __syncwarp();
+        }
+        for (uint32_t i = istart; i < i1; i++) {
             const int32_t slot = rsqf_insert(f, q, fps[i]);
             if (f.crossed) break;
             if (lane == 0) ret[i] = slot;
@@ -237,7 +278,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_rsqf_round_warp(
 // blocks restored from t0 in place.
 __global__ void k_rsqf_round_big(uint8_t *t, const uint8_t *t0, uint32_t nblocks, uint32_t q, const uint32_t *fps,
                                  const uint32_t *fhome, const uint32_t *blist, const uint32_t *counts,
-                                 uint8_t *crossed, uint32_t *n_crossed, int32_t *ret, int t0_zero)
+                                 uint8_t *crossed, uint32_t *n_crossed, int32_t *ret, int t0_zero,
+                                 const uint8_t *sus, const uint32_t *fpos)
 {
     const uint32_t ng = counts[2];
     for (uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ng; gi += gridDim.x * blockDim.x) {
@@ -245,8 +287,23 @@ __global__ void k_rsqf_round_big(uint8_t *t, const uint8_t *t0, uint32_t nblocks
         for (size_t i = (size_t)b * RSQF_BB; i < (size_t)e * RSQF_BB; i++) t[i] = t0[i];
         RsqfGroupTable f{t, t0, nblocks, b, e, false, t0_zero != 0};
         const uint32_t i0 = fhome[min(b, nblocks)], i1 = fhome[min(e, nblocks)];
+        uint32_t istart = i0;
+        if (sus) {  // a build: as in k_rsqf_round_warp, on the packed blocks
+            istart = rsqf_replay_start(sus, fpos, b, min(e, nblocks), i0, i1);
+            for (uint32_t i = i0; i < istart; i++) {
+                const uint32_t fp = fps[i], s = (uint32_t)ret[i];
+                const uint32_t blk = s / RSQF_SPB, sl = s % RSQF_SPB, hq = (fp >> RSQF_R);
+                f.set_occ(hq / RSQF_SPB, f.occ(hq / RSQF_SPB) | (1ull << (hq % RSQF_SPB)));
+                if (i + 1 == istart || (fps[i + 1] >> RSQF_R) != hq) f.set_re(blk, f.re(blk) | (1ull << sl));
+                f.set_rem(blk, sl, fp & RSQF_RMASK);
+            }
+            for (uint32_t blk = b; blk < e && blk < nblocks; blk++) {
+                const uint32_t hi = min(fhome[blk], istart), lo = max(fpos[blk], i0);
+                f.set_off(blk, hi > lo ? hi - lo : 0u);
+            }
+        }
         bool cross = false;
-        for (uint32_t i = i0; i < i1; i++) {
+        for (uint32_t i = istart; i < i1; i++) {
             const int32_t slot = rsqf_insert(f, q, fps[i]);
             if (f.crossed) {
                 cross = true;
@@ -402,10 +459,12 @@ int GQF_RSQF_API(lookup_sorted)(const gqf_rsqf *cqf, int n, const uint32_t *d_ke
 //    (k_rsqf_round); a group whose writes leave it is merged with its
 //    successor and replayed from the pre-batch table until none does.
 // Return slots are indexed by sorted position, as the reference's are.
+// sus / fpos: a build into an empty filter (replays start after the
+// canonical prefix of each group); null for incremental batches.
 static int rsqf_replay_rounds(uint8_t *t, const uint8_t *t0, uint32_t nbl, uint32_t q, const uint32_t *items,
                               const uint32_t *fhome, uint8_t *start, uint8_t *active, uint8_t *crossed,
                               uint32_t *wlist, uint32_t *blist, uint32_t *ctr, int32_t *d_ret, bool t0_zero,
-                              cudaStream_t s)
+                              cudaStream_t s, const uint8_t *sus = nullptr, const uint32_t *fpos = nullptr)
 {
     const DeviceInfo &di = device_info(current_device());
     const uint32_t grid = std::min<uint32_t>((nbl + 1 + 255) / 256, di.sms * 8);
@@ -414,12 +473,12 @@ static int rsqf_replay_rounds(uint8_t *t, const uint8_t *t0, uint32_t nbl, uint3
         k_rsqf_groups<<<grid, 256, 0, s>>>(nbl, start, active, fhome, wlist, wlist + 2 * (size_t)(nbl + 1), blist,
                                            ctr);
         k_rsqf_round_warp<RSQF_SMALL_GROUP, 8><<<di.sms * 8, 256, 0, s>>>(t, t0, nbl, q, items, fhome, wlist, ctr,
-                                                                        crossed, ctr + 3, d_ret, t0_zero ? 1 : 0);
+                                                                        crossed, ctr + 3, d_ret, t0_zero ? 1 : 0, sus, fpos);
         k_rsqf_round_warp<RSQF_WARP_GROUP_MAX, 1><<<di.sms * 16, 32, 0, s>>>(
             t, t0, nbl, q, items, fhome, wlist + 2 * (size_t)(nbl + 1), ctr + 1, crossed, ctr + 3, d_ret,
-            t0_zero ? 1 : 0);
+            t0_zero ? 1 : 0, sus, fpos);
         k_rsqf_round_big<<<std::max(1, di.sms), 64, 0, s>>>(t, t0, nbl, q, items, fhome, blist, ctr, crossed,
-                                                             ctr + 3, d_ret, t0_zero ? 1 : 0);
+                                                             ctr + 3, d_ret, t0_zero ? 1 : 0, sus, fpos);
         count_launches(4);
         uint32_t h_n = 0;
         GQF_CK(cudaMemcpyAsync(&h_n, ctr + 3, 4, cudaMemcpyDeviceToHost, s));
@@ -510,7 +569,7 @@ int GQF_RSQF_API(insert)(const gqf_rsqf *cqf, int n, const uint32_t *d_keys, int
                 k_rsqf_mark_sus<<<grid, 256, 0, s>>>(nbl, start, sus, active);
                 count_launches(1);
                 st = rsqf_replay_rounds(table, t0, nbl, q, items, fhome, start, active, crossed, wlist, blist, ctr,
-                                        d_ret, true, s);
+                                        d_ret, true, s, sus, fpos);
                 if (st) return st;
             }
         } else {

@@ -330,6 +330,59 @@ def test_rsqf8_oracle_vs_reference(q, alpha, seed, order):
         R.ref_rsqf_free(f)
 
 
+@pytest.mark.parametrize("rbits", [5, 8])
+def test_rsqf_sorted_build_canonical_prefix(rbits):
+    """The engine's build replays a cluster holding a block of canonical
+    offset above 62 only from the first item positioned in the first such
+    block S1, after writing the earlier items' canonical state.  This pins
+    that on the oracle (the reference's sequential insert): in random fills
+    with hot quotient ranges, inserting the items before fpos[S1] in
+    ascending order gives the cluster's items before S1 exactly their
+    canonical positions and blocks."""
+    rng = np.random.default_rng(11 + rbits)
+    clusters = 0
+    for trial in range(60):
+        q = int(rng.integers(9, 12))
+        seed = int(rng.integers(0, 1 << 30))
+        base = O.mt_keys(seed, int(rng.uniform(0.5, 0.93) * (1 << q)))
+        cand = O.mt_keys(seed + 1, 40 << q >> 6 << 6)
+        f = O.aphash(cand, q, rbits)
+        hot = []
+        for _ in range(int(rng.integers(1, 4))):
+            lo = int(rng.integers(0, 1 << q))
+            hot.append(cand[((f >> rbits) >= lo) & ((f >> rbits) < lo + int(rng.integers(10, 60)))]
+                       [:int(rng.integers(60, 250))])
+        keys = np.concatenate([base] + hot)
+        fps = O.aphash(keys, q, rbits).astype(np.int64)
+        o = np.argsort(fps, kind="stable")
+        ks, fps = keys[o], fps[o]
+        i = np.arange(fps.size)
+        qs = fps >> rbits
+        pos = i + np.maximum.accumulate(qs - i)
+        nbl = (1 << q) // 64 + 1
+        if pos[-1] >= nbl * 64:
+            continue
+        B = np.arange(nbl + 1)
+        fhome, fpos = np.searchsorted(qs, 64 * B), np.searchsorted(pos, 64 * B)
+        off = fhome - fpos
+        starts = np.nonzero(off == 0)[0]
+        bb = 17 + 8 * rbits
+        for s1 in np.nonzero(off > 62)[0]:
+            b = starts[np.searchsorted(starts, s1, side="right") - 1]
+            if np.any(off[b:s1] > 62):
+                continue  # not the cluster's first such block
+            istar = int(fpos[s1])
+            t = O.rsqf_new(q, rbits)
+            rets = O.rsqf_insert_sorted(t, q, ks[:istar], rbits)
+            c = O.rsqf_new(q, rbits)
+            assert O.rsqf_layout_sorted(c, q, fps[:istar].astype(np.uint32), rbits) == 0
+            i0 = int(fhome[b])  # this cluster's items (earlier clusters may be past their own S1)
+            assert np.array_equal(rets[i0:], pos[i0:istar]), (trial, q)
+            assert np.array_equal(t[b * bb:s1 * bb + bb], c[b * bb:s1 * bb + bb]), (trial, q)
+            clusters += 1
+    assert clusters > 20
+
+
 def test_rsqf_sorted_build_canonical_below_offset_63():
     """The engine writes an empty-filter batch from canonical positions
     wherever every block offset stays <= 62 and replays the rest.  This pins
