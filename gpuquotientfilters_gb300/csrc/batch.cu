@@ -320,7 +320,8 @@ static int mf_create(Batch *b, const gqf_sqf_job *jobs, int count, int no_duplic
     uint64_t n_items = 0, fix_total = 0;
     for (int i = 0; i < count; i++) {
         const gqf_sqf &f = jobs[i].filter;
-        if (!f.table || f.rbits != b->r || f.bytesPerElement != b->bpe || f.qbits < 7 || f.qbits + f.rbits > 31)
+        if (!f.table || (reinterpret_cast<uintptr_t>(f.table) & 15u) || f.rbits != b->r ||
+            f.bytesPerElement != b->bpe || f.qbits < 7 || f.qbits + f.rbits > 31)
             return GQF_ERR_ARG;
         if (jobs[i].n_build < 0 || jobs[i].n_lookup < 0) return GQF_ERR_ARG;
         if (jobs[i].n_build > 0 && !jobs[i].d_build_keys) return GQF_ERR_ARG;

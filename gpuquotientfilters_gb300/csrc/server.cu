@@ -223,7 +223,7 @@ static int srv_create(Server *S, const gqf_sqf *filters, int nf, const gqf_serve
     size_t tables = 0, ws = 0;
     for (int i = 0; i < nf; i++) {
         const gqf_sqf &f = filters[i];
-        if (!f.table) return GQF_ERR_ARG;
+        if (!f.table || (reinterpret_cast<uintptr_t>(f.table) & 15u)) return GQF_ERR_ARG;
         tables += align_up(gqf_sqf_table_bytes(f.qbits, f.rbits), 256);
         ws = std::max(ws, gqf_sqf_update_workspace_bytes(f.qbits, f.rbits, S->cfg.max_op_keys));
     }

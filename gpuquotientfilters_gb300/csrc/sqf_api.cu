@@ -10,6 +10,7 @@
 #include "sqf_build.cuh"
 #include "sqf_extract.cuh"
 #include "sqf_lookup.cuh"
+#include "sqf_mirror.cuh"
 
 namespace gqf {
 
@@ -529,26 +530,27 @@ static int lookup_unsorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uin
     const SqfGeom tg = geom_of(qf);
     Arena &ar = arena(current_device(), s);
     std::lock_guard<std::mutex> lk(ar.mu);
-    // one-byte slots and a batch of at least one query per 16 slots: build the
-    // pending-run summary (one byte per 8 slots) first
-    const uint32_t nwords = (tg.nslots + 7) / 8;
-    const bool summary = BPE == 1 && (uint64_t)n * 16 >= tg.nslots;
-    uint8_t *sum = nullptr;
-    if (summary) {
-        sum = static_cast<uint8_t *>(arena_reserve(ar, align_up((size_t)nwords, 256)));
-        if (!sum) return GQF_ERR_NOMEM;
+    // one-byte slots and a batch of at least one query per 16 slots: transpose
+    // the table into the bit-plane mirror first
+    const bool mirror = BPE == 1 && (uint64_t)n * 16 >= tg.nslots;
+    uint4 *rec = nullptr;
+    if (mirror) {
+        rec = static_cast<uint4 *>(arena_reserve(ar, mir_bytes(tg.nslots)));
+        if (!rec) return GQF_ERR_NOMEM;
+        GQF_CK(set_smem(k_sqf_mirror, 2 * (size_t)MIR_TILE));
     }
     int st = call_begin(ar, s, ms != nullptr);
     if (st) return st;
     TableView v{qf->table, tg.q, tg.r, tg.nslots, (uint32_t)tg.T, (uint32_t)(tg.T / 8)};
-    if (n > 0 && summary) {
+    if (n > 0 && mirror) {
         const DeviceInfo &di = device_info(current_device());
-        const uint32_t tiles = (nwords + PS_THREADS * PS_WPT - 1) / (PS_THREADS * PS_WPT);
-        k_pending_summary<<<tiles, PS_THREADS, 0, s>>>(v, sum);
-        constexpr int QPT = 2;
-        const uint32_t per_block = LOOKUP_THREADS * QPT;
-        const uint32_t grid = std::min<uint32_t>((n + per_block - 1) / per_block, (uint32_t)di.sms * 32);
-        k_lookup_unsorted_sum<QPT><<<grid, LOOKUP_THREADS, 0, s>>>(keys, (uint32_t)n, v, sum, out);
+        const uint32_t ngroups = mir_groups(tg.nslots);
+        const uint32_t ntiles = (uint32_t)(((uint64_t)(ngroups + 1) * MIR_SLOTS + MIR_TILE - 1) / MIR_TILE);
+        k_sqf_mirror<<<std::min<uint32_t>(ntiles, (uint32_t)di.sms * 3), MIR_BUILD_THREADS, 2 * MIR_TILE, s>>>(
+            v, rec, ngroups, ntiles, ar.err);
+        const uint32_t grid = std::min<uint32_t>((n + MIR_LOOKUP_THREADS - 1) / MIR_LOOKUP_THREADS,
+                                                 (uint32_t)di.sms * 32);
+        k_lookup_mirror<<<grid, MIR_LOOKUP_THREADS, 0, s>>>(keys, (uint32_t)n, v, rec, out);
         count_launches(2);
     } else if (n > 0) {
         const DeviceInfo &di = device_info(current_device());
@@ -570,7 +572,7 @@ static int lookup_sorted_t(const gqf_sqf *qf, int n, const uint32_t *keys, uint3
     // Results go to the queries' input positions either way (the reference
     // sorts them back by index, quotientFilter.cu:304-305).  On one-byte slots
     // a batch of at least one query per 16 slots is answered faster through
-    // the pending-run summary than by bucketing the queries first.
+    // the bit-plane mirror than by bucketing the queries first.
     if (BPE == 1 && (uint64_t)n * 16 >= tg.nslots) return lookup_unsorted_t<BPE>(qf, n, keys, out, s, ms);
     LayoutPlan p = plan_layout(tg.q, tg.r, (uint64_t)tg.nslots * 8 / 10, (uint64_t)n, false);
     // query buckets: aim for ~4k queries per bucket, table-aligned
@@ -720,7 +722,12 @@ int gqf_sqf_free(gqf_sqf *qf)
     return GQF_OK;
 }
 
-static bool sqf_ok(const gqf_sqf *qf) { return qf && qf->table && qr_ok(qf->qbits, qf->rbits); }
+// the kernels read the table in aligned 8- and 16-byte words and bulk copies
+static bool table_aligned(const void *t) { return (reinterpret_cast<uintptr_t>(t) & 15u) == 0; }
+static bool sqf_ok(const gqf_sqf *qf)
+{
+    return qf && qf->table && table_aligned(qf->table) && qr_ok(qf->qbits, qf->rbits);
+}
 
 int gqf_sqf_bulk_build(const gqf_sqf *qf, int n, const uint32_t *d_keys, int no_duplicates, void *stream, float *ms)
 {

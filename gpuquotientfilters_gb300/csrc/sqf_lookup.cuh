@@ -52,11 +52,9 @@ QF_HD uint64_t ld_word(const TableView &v, uint32_t w)
 //   3. forward: fq's run is the (D+1)-th run start at or after fq;
 //   4. the run's elements in slot order up to the first remainder >= fr:
 //      equal -> its slot, greater or end of run -> miss.
-// x0 = the home word, loaded by the caller so several queries' first loads
-// can be in flight together.  P, when in [0, 255), is the count D at the home
-// word's first slot (the pending-run summary below); it replaces the walk
-// back past the home word.
-QF_HD uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr, uint64_t x, int P = -1)
+// x = the home word, loaded by the caller so several queries' first loads
+// can be in flight together.
+QF_HD uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr, uint64_t x)
 {
     constexpr uint64_t OCC = 0x0404040404040404ull;  // occupied bit of every byte
     const uint32_t w = fq >> 3, k = fq & 7u;
@@ -69,8 +67,6 @@ QF_HD uint32_t sqf_query_b1(const TableView &v, uint32_t fq, uint32_t fr, uint64
     if (st) {
         const uint64_t R = below & ~bytes_below(highest_byte(st));
         D = popc64(x & OCC & R) - popc64(rs & R);
-    } else if (P >= 0 && P < 255) {
-        D = P + popc64(x & OCC & below) - popc64(rs & below);
     } else {
         D = popc64(x & OCC & below) - popc64(rs & below);
         for (int ww = (int)w - 1; ww >= 0; ww--) {
@@ -216,148 +212,6 @@ __global__ void __launch_bounds__(LOOKUP_THREADS) k_lookup_unsorted(const uint32
             const uint32_t res = BPE == 1 ? sqf_query_b1(v, (fp[k] >> v.r) & qmask, fp[k] & rmask, x[k])
                                           : sqf_query<BPE>(v, fp[k]);
             out[b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x] = res;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------
-// Pending-run summary for unsorted lookups on one-byte slots.  P(w) = the
-// lookup's D at slot 8w: the runs of quotients below 8w still pending there.
-// Along the table, P(w + 1) = a_w when word w holds an unshifted slot (the
-// count from the last one to the word's end), else P(w) + b_w (the count over
-// the word) -- a map P -> r ? a : P + b, and maps compose.  A tile of 2048
-// words takes its entry value from the walk back before it (one warp, almost
-// always one round), scans its threads' maps, and writes P as one byte per
-// word, 255 meaning "walk back instead".  A lookup then reads its home
-// word's byte instead of walking back past that word, so no lane of a warp
-// waits on another's long cluster.
-// ---------------------------------------------------------------------
-constexpr int PS_THREADS = 256, PS_WPT = 8;  // 2048 words a tile
-
-struct PendFn8 {
-    uint32_t r;  // reset: the word range holds an unshifted slot
-    int a, b;    // r ? a : P + b
-};
-QF_HD PendFn8 pend_compose(PendFn8 f, PendFn8 g)  // f, then g
-{
-    PendFn8 h;
-    h.r = f.r | g.r;
-    h.a = g.r ? g.a : f.a + g.b;
-    h.b = f.b + g.b;
-    return h;
-}
-QF_HD int pend_apply(PendFn8 f, int P) { return f.r ? f.a : P + f.b; }
-QF_HD PendFn8 pend_word(uint64_t x)
-{
-    constexpr uint64_t OCC = 0x0404040404040404ull;
-    const uint64_t st = bl_unshifted(x), rs = bl_run_starts(x);
-    PendFn8 f;
-    if (st) {
-        const uint64_t R = ~bytes_below(highest_byte(st));
-        f.r = 1;
-        f.a = popc64(x & OCC & R) - popc64(rs & R);
-        f.b = 0;
-    } else {
-        f.r = 0;
-        f.a = 0;
-        f.b = popc64(x & OCC) - popc64(rs);
-    }
-    return f;
-}
-
-static __global__ void __launch_bounds__(PS_THREADS) k_pending_summary(TableView v, uint8_t *__restrict__ sum)
-{
-    __shared__ PendFn8 s_w[PS_THREADS / 32];
-    __shared__ int s_pin;
-    const uint32_t nwords = (v.nslots + 7) >> 3;
-    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const uint32_t w0 = blockIdx.x * (PS_THREADS * PS_WPT) + tid * PS_WPT;
-    if (wid == 0) {
-        const uint32_t x0 = blockIdx.x * (PS_THREADS * PS_WPT) * 8u;
-        const int P = x0 < v.nslots ? pending_runs_warp(v.t, x0) : 0;
-        if (lane == 0) s_pin = P;
-    }
-    PendFn8 fw[PS_WPT];  // the words' maps, kept for the output pass
-    if (w0 + PS_WPT <= v.nwords_full && (reinterpret_cast<uintptr_t>(v.t) & 15u) == 0) {
-        const uint4 *p4 = reinterpret_cast<const uint4 *>(v.t + 8ull * w0);
-#pragma unroll
-        for (int k = 0; k < PS_WPT / 2; k++) {
-            const uint4 q4 = __ldg(p4 + k);
-            fw[2 * k] = pend_word((uint64_t)q4.x | ((uint64_t)q4.y << 32));
-            fw[2 * k + 1] = pend_word((uint64_t)q4.z | ((uint64_t)q4.w << 32));
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < PS_WPT; k++) fw[k] = pend_word(w0 + k < nwords ? ld_word(v, w0 + k) : 0ull);
-    }
-    PendFn8 f = fw[0];
-#pragma unroll
-    for (int k = 1; k < PS_WPT; k++) f = pend_compose(f, fw[k]);
-    // exclusive scan of the thread maps across the block
-    PendFn8 incl = f;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        PendFn8 p;
-        p.r = __shfl_up_sync(0xffffffffu, incl.r, o);
-        p.a = __shfl_up_sync(0xffffffffu, incl.a, o);
-        p.b = __shfl_up_sync(0xffffffffu, incl.b, o);
-        if (lane >= o) incl = pend_compose(p, incl);
-    }
-    PendFn8 excl;
-    excl.r = __shfl_up_sync(0xffffffffu, incl.r, 1);
-    excl.a = __shfl_up_sync(0xffffffffu, incl.a, 1);
-    excl.b = __shfl_up_sync(0xffffffffu, incl.b, 1);
-    if (lane == 0) excl = PendFn8{0u, 0, 0};
-    if (lane == 31) s_w[wid] = incl;
-    __syncthreads();
-    PendFn8 wex{0u, 0, 0};
-    for (uint32_t w = 0; w < wid; w++) wex = pend_compose(wex, s_w[w]);
-    int P = pend_apply(pend_compose(wex, excl), s_pin);
-    uint64_t out = 0;
-#pragma unroll
-    for (int k = 0; k < PS_WPT; k++) {
-        out |= (uint64_t)(P < 0 ? 255u : (P > 254 ? 255u : (uint32_t)P)) << (8 * k);
-        P = pend_apply(fw[k], P);
-    }
-    if (w0 + PS_WPT <= nwords) {
-        *reinterpret_cast<uint64_t *>(sum + w0) = out;
-    } else {
-        for (int k = 0; k < PS_WPT && w0 + k < nwords; k++) sum[w0 + k] = (uint8_t)(out >> (8 * k));
-    }
-}
-
-// launchUnsortedLookups on one-byte slots with the pending-run summary.
-template <int QPT>
-__global__ void __launch_bounds__(LOOKUP_THREADS) k_lookup_unsorted_sum(const uint32_t *__restrict__ keys, uint32_t n,
-                                                                       TableView v, const uint8_t *__restrict__ sum,
-                                                                       uint32_t *__restrict__ out)
-{
-    const uint32_t fpmask = (v.q + v.r >= 32) ? 0xFFFFFFFFu : ((1u << (v.q + v.r)) - 1u);
-    const uint32_t qmask = (1u << v.q) - 1u, rmask = (1u << v.r) - 1u;
-    const uint32_t per_block = LOOKUP_THREADS * QPT;
-    for (uint64_t b0 = (uint64_t)blockIdx.x * per_block; b0 < n; b0 += (uint64_t)gridDim.x * per_block) {
-        uint32_t fp[QPT];
-        bool valid[QPT];
-#pragma unroll
-        for (int k = 0; k < QPT; k++) {
-            const uint64_t i = b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x;
-            valid[k] = i < n;
-            fp[k] = valid[k] ? __ldg(keys + i) : 0u;
-        }
-        uint64_t x[QPT];
-        int P[QPT];
-#pragma unroll
-        for (int k = 0; k < QPT; k++) {
-            fp[k] = aphash32(fp[k]) & fpmask;
-            const uint32_t w = ((fp[k] >> v.r) & qmask) >> 3;
-            x[k] = valid[k] ? ld_word(v, w) : 0ull;
-            P[k] = valid[k] ? (int)__ldg(sum + w) : 255;
-        }
-#pragma unroll
-        for (int k = 0; k < QPT; k++) {
-            if (!valid[k]) continue;
-            out[b0 + (uint64_t)k * LOOKUP_THREADS + threadIdx.x] =
-                sqf_query_b1(v, (fp[k] >> v.r) & qmask, fp[k] & rmask, x[k], P[k]);
         }
     }
 }

@@ -25,7 +25,7 @@ extern "C" {
 
 typedef enum gqf_status {
     GQF_OK = 0,
-    GQF_ERR_ARG = 1,       /* bad q/r, null pointer, negative count        */
+    GQF_ERR_ARG = 1,       /* bad q/r, null or unaligned pointer, negative count */
     GQF_ERR_FULL = 2,      /* layout needs more than (1<<q)*1.1 slots       */
     GQF_ERR_CUDA = 3,      /* a CUDA runtime call failed                    */
     GQF_ERR_TIMEOUT = 4,   /* a bounded device-side wait ran out            */
@@ -42,7 +42,8 @@ typedef struct gqf_sqf {
     unsigned int qbits;
     unsigned int rbits;
     unsigned int bytesPerElement;
-    unsigned char *table; /* device, calcNumSlotsGPU(q, r) bytes */
+    unsigned char *table; /* device, calcNumSlotsGPU(q, r) bytes, 16-byte aligned
+                           * (cudaMalloc gives 256); others return GQF_ERR_ARG */
 } gqf_sqf;
 
 /* Rank-and-select filter handle: identical to `struct
@@ -101,9 +102,10 @@ int gqf_sqf_bulk_build(const gqf_sqf *qf, int n, const uint32_t *d_keys,
                        int no_duplicates, void *stream, float *ms);
 
 /* launchUnsortedLookups, quotientFilter.cu:359-381: d_out[i] = slot of
- * key i's remainder, or GQF_NOT_FOUND.  A batch of at least one query per 16
- * slots first scans the table into a per-8-slot summary (stream workspace,
- * slots / 8 bytes) so no query walks back past its home word. */
+ * key i's remainder, or GQF_NOT_FOUND.  On one-byte slots a batch of at least
+ * one query per 16 slots first transposes the table into a bit-plane mirror
+ * (stream workspace, 32 bytes per 31 slots) and answers each query from two
+ * of its 32-byte records. */
 int gqf_sqf_lookup_unsorted(const gqf_sqf *qf, int n, const uint32_t *d_keys,
                             uint32_t *d_out, void *stream, float *ms);
 

@@ -2,12 +2,15 @@
 // code's own function, compiled for the host) over a table and a list of
 // fingerprints read from files, and writes the results.  Used by the CPU
 // tests to check the byte-lane SWAR walk against the oracle without a GPU.
+// With SWAR_MIRROR set, the queries go through the bit-plane mirror instead
+// (mirror_record / mirror_query, the lookup kernel's own functions), falling
+// back to sqf_query_b1 where the two-record window does not decide.
 //   swar_query_host <table.bin> <fps.bin> <q> <r> <nslots> <out.bin>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 
-#include "../../gpuquotientfilters_gb300/csrc/sqf_lookup.cuh"
+#include "../../gpuquotientfilters_gb300/csrc/sqf_mirror.cuh"
 
 static std::vector<unsigned char> slurp(const char *path)
 {
@@ -35,23 +38,47 @@ int main(int argc, char **argv)
     gqf::TableView v{tab.data(), q, r, nslots, (uint32_t)tab.size(), (uint32_t)(tab.size() / 8)};
     const size_t n = fpb.size() / 4;
     const uint32_t *fps = reinterpret_cast<const uint32_t *>(fpb.data());
-    // with SWAR_SUMMARY set, each query gets its home word's pending-run
-    // summary byte (the recurrence the summary kernel scans)
-    const bool use_sum = std::getenv("SWAR_SUMMARY") != nullptr;
-    std::vector<int> P;
-    if (use_sum) {
-        const uint32_t nwords = (nslots + 7) / 8;
-        P.resize(nwords);
-        int p = 0;
-        for (uint32_t w = 0; w < nwords; w++) {
-            P[w] = p < 0 || p > 254 ? 255 : p;
-            p = gqf::pend_apply(gqf::pend_word(gqf::ld_word(v, w)), p);
-        }
-    }
     std::vector<uint32_t> out(n);
+    if (std::getenv("SWAR_MIRROR")) {
+        const uint32_t ng = gqf::mir_groups(nslots);
+        std::vector<uint32_t> rec((size_t)(ng + 1) * 8);
+        int D = 0;  // pending runs at the group's first slot
+        for (uint32_t G = 0; G <= ng; G++) {
+            uint32_t r[8];
+            gqf::mirror_record(tab.data(), (uint32_t)tab.size(), G, D, r);
+            for (int w = 0; w < 8; w++) rec[(size_t)G * 8 + w] = r[w];
+            for (uint32_t j = 0; j < gqf::MIR_SLOTS; j++) {
+                const size_t sl = (size_t)G * gqf::MIR_SLOTS + j;
+                const uint32_t e = sl < tab.size() ? tab[sl] : 0u;
+                D += (int)((e >> 2) & 1u) - (int)((e & 7u) != 0 && !((e >> 1) & 1u));
+            }
+        }
+        size_t undecided = 0;
+        for (size_t i = 0; i < n; i++) {
+            const uint32_t fq = (fps[i] >> r) & ((1u << q) - 1u), fr = fps[i] & ((1u << r) - 1u);
+            const uint32_t G = fq / gqf::MIR_SLOTS;
+            uint32_t r0[8], r1[8];
+            for (int w = 0; w < 8; w++) {
+                r0[w] = rec[(size_t)G * 8 + w];
+                r1[w] = rec[(size_t)(G + 1) * 8 + w];
+            }
+            uint32_t res = gqf::mirror_query(fq, fr, fq - G * gqf::MIR_SLOTS, r0, r1);
+            if (res == gqf::MIRROR_UNDECIDED) {
+                undecided++;
+                res = gqf::sqf_query_b1(v, fq, fr, gqf::ld_word(v, fq >> 3));
+            }
+            out[i] = res;
+        }
+        std::fprintf(stderr, "undecided %zu of %zu\n", undecided, n);
+        FILE *f = std::fopen(argv[6], "wb");
+        if (!f) return 4;
+        std::fwrite(out.data(), 4, n, f);
+        std::fclose(f);
+        return 0;
+    }
     for (size_t i = 0; i < n; i++) {
         const uint32_t fq = (fps[i] >> r) & ((1u << q) - 1u), fr = fps[i] & ((1u << r) - 1u);
-        out[i] = gqf::sqf_query_b1(v, fq, fr, gqf::ld_word(v, fq >> 3), use_sum ? P[fq >> 3] : -1);
+        out[i] = gqf::sqf_query_b1(v, fq, fr, gqf::ld_word(v, fq >> 3));
     }
     FILE *f = std::fopen(argv[6], "wb");
     if (!f) return 4;

@@ -59,3 +59,18 @@ def test_workload_config1_shapes(gqf):
     assert np.isin(c["lookups"], c["keys"]).sum() >= 19661 // 2
     assert W.n_keys(15, 0.6) == 19661 and W.n_keys(15, 0.6, reference_arithmetic=True) == 19660
     assert W.n_keys(26, 0.8) == 53687091 and W.n_keys(26, 0.8, reference_arithmetic=True) == 53687092
+
+
+def test_unaligned_table_refused_before_any_device_call(gqf):
+    """A table pointer that is not 16-byte aligned is refused with
+    GQF_ERR_ARG by the argument check itself (no CUDA call is made, so this
+    runs without a GPU)."""
+    L = gqf.lib()
+    for addr in (0x10001, 0x10008, 0x1000C):
+        qf = gqf.quotient_filter(20, 5, 1, addr)
+        keys, out = 0x20000, 0x30000
+        assert L.gqf_sqf_lookup_unsorted(C.byref(qf), 1 << 20, C.c_void_p(keys), C.c_void_p(out), None, None) == 1
+        assert L.gqf_sqf_lookup_sorted(C.byref(qf), 16, C.c_void_p(keys), C.c_void_p(out), None, None) == 1
+        assert L.gqf_sqf_insert(C.byref(qf), 16, C.c_void_p(keys), None, None) == 1
+        assert L.gqf_sqf_delete(C.byref(qf), 16, C.c_void_p(keys), None, None) == 1
+        assert L.gqf_sqf_bulk_build(C.byref(qf), 16, C.c_void_p(keys), 1, None, None) == 1

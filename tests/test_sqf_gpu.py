@@ -111,6 +111,42 @@ def test_build_and_lookups(gqf, cuda, q, r, alpha, seed, nodup):
     assert np.array_equal(f.lookup(small, sorted_=True), ws)
 
 
+@pytest.mark.parametrize("q,alpha,nodup", [(17, 0.8, True), (19, 0.95, False)])
+def test_large_lookups_and_table_alignment(gqf, cuda, q, alpha, nodup):
+    """Large one-byte-slot batches go through the bit-plane mirror (its
+    records are read and written as 32-byte sectors, the table by bulk
+    copies).  A filter whose table is not 16-byte aligned (a drop-in caller's
+    own buffer at an odd address) is refused on the host with GQF_ERR_ARG
+    before any kernel runs."""
+    r = 5
+    n = int(alpha * (1 << q))
+    keys = O.mt_keys(40 + q, n)
+    f = Filter(gqf, cuda, q, r)
+    f.build(keys, nodup)
+    t = oracle_build(q, r, keys, nodup)
+    look = np.concatenate([keys[: n // 2], O.mt_keys(41 + q, n // 2, skip=n)])
+    want = O.sqf_lookup(t, q, r, look)
+    assert np.array_equal(f.lookup(look), want)
+    assert np.array_equal(f.lookup(look, sorted_=True), want)
+    # the same table at an offset of 16 bytes answers the same
+    T = t.size
+    buf = cuda.zeros(T + 64, dtype=cuda.uint8, device="cuda")
+    buf[16:16 + T] = cuda.from_numpy(t).cuda()
+    moved = gqf.quotient_filter(q, r, 1, buf.data_ptr() + 16)
+    out = cuda.empty(look.size, dtype=cuda.int32, device="cuda")
+    gqf.launchUnsortedLookups(moved, look.size, to_dev(cuda, look), out)
+    assert np.array_equal(from_dev(out), want)
+    # an odd address is refused
+    odd = gqf.quotient_filter(q, r, 1, buf.data_ptr() + 1)
+    for call in (lambda: gqf.launchUnsortedLookups(odd, look.size, to_dev(cuda, look), out),
+                 lambda: gqf.launchSortedLookups(odd, look.size, to_dev(cuda, look), out),
+                 lambda: gqf.insert(odd, 16, to_dev(cuda, keys[:16])),
+                 lambda: gqf.bulkBuildSegmentedLayouts(odd, 16, to_dev(cuda, keys[:16]), True)):
+        with pytest.raises(gqf.GQFError) as ei:
+            call()
+        assert ei.value.status == 1
+
+
 def test_build_reference_arithmetic_count(gqf, cuda):
     from gpuquotientfilters_gb300 import workload as W
     q, r = 15, 5

@@ -1,11 +1,12 @@
-"""CPU check of the one-byte-slot query walk that the lookup kernels run.
+"""CPU check of the one-byte-slot query walks that the lookup kernels run.
 
-The state machine (sqf_query_init / sqf_query_step in
-gpuquotientfilters_gb300/csrc/sqf_lookup.cuh) is host+device code; here it is
-compiled for the host by nvcc and run over tables made by the oracle, and its
-results must equal the oracle's lookups (the reference's hashAndLookUp,
-quotientFilter.cu:320-357) on every query, at fills up to 0.95, with and
-without duplicate fingerprints, after deletes, and near the table's end."""
+The byte-lane walk (sqf_query_b1 in gpuquotientfilters_gb300/csrc/sqf_lookup.cuh)
+and the bit-plane mirror (mirror_record / mirror_query in sqf_mirror.cuh) are
+host+device code; here they are compiled for the host by nvcc and run over
+tables made by the oracle, and their results must equal the oracle's lookups
+(the reference's hashAndLookUp, quotientFilter.cu:320-357) on every query, at
+fills up to 1.0, with and without duplicate fingerprints, after deletes, near
+the table's ends, and where the pending-run count saturates."""
 import os
 import shutil
 import subprocess
@@ -33,13 +34,13 @@ def driver(tmp_path_factory):
     return exe
 
 
-def run_driver(exe, tmp_path, t, q, r, fps, summary=False):
+def run_driver(exe, tmp_path, t, q, r, fps, mirror=False):
     tf, ff, of = tmp_path / "t.bin", tmp_path / "f.bin", tmp_path / "o.bin"
     t.tofile(tf)
     np.ascontiguousarray(fps, np.uint32).tofile(ff)
     env = dict(os.environ)
-    if summary:
-        env["SWAR_SUMMARY"] = "1"
+    if mirror:
+        env["SWAR_MIRROR"] = "1"
     p = subprocess.run([exe, str(tf), str(ff), str(q), str(r), str(O.sqf_num_slots(q)), str(of)],
                        capture_output=True, text=True, env=env)
     assert p.returncode == 0, p.stderr
@@ -60,13 +61,15 @@ def test_walk_matches_oracle(driver, tmp_path, q, fill, nodup):
     want = O.sqf_lookup(t, q, r, look)
     got = run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r))
     assert np.array_equal(got, want)
-    # the same walk starting from the pending-run summary of the home word
-    got = run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r), summary=True)
+    # the bit-plane mirror's two-record window, the walk where it is undecided
+    got = run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r), mirror=True)
     assert np.array_equal(got, want)
     # every fingerprint of the quotient space near the table's start and end
     allq = np.arange(1 << (q + r), dtype=np.uint32)
     edge = np.concatenate([allq[: 64 << r], allq[-(64 << r):]])
-    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, edge), _oracle_fp_lookup(t, q, r, edge))
+    want_edge = _oracle_fp_lookup(t, q, r, edge)
+    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, edge), want_edge)
+    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, edge, mirror=True), want_edge)
 
 
 def _oracle_fp_lookup(t, q, r, fps):
@@ -112,4 +115,24 @@ def test_walk_after_deletes(driver, tmp_path):
     O.sqf_bulk_build(t, q, r, keys, True)
     O.sqf_delete(t, q, r, keys[: n // 3])
     look = np.concatenate([keys, O.mt_keys(78, n // 2)])
-    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r)), O.sqf_lookup(t, q, r, look))
+    want = O.sqf_lookup(t, q, r, look)
+    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r)), want)
+    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, O.aphash(look, q, r), mirror=True), want)
+
+
+def test_mirror_saturated_pending_count(driver, tmp_path):
+    """A cluster with more than 254 runs pending: the mirror records carry
+    P = 255 there and those queries fall back to the full walk."""
+    q, r = 12, 5
+    fps = [(5 << r) | (i * 32 // 300) for i in range(300)]      # one run of 300 at quotient 5
+    fps += [(qq << r) | 7 for qq in range(6, 306)]             # 300 runs pushed behind it
+    fps += [(qq << r) | 3 for qq in range(1000, 1040, 3)]      # a separate sparse region
+    fps = np.array(sorted(fps), np.uint32)
+    t = O.sqf_new(q, r)
+    assert O.sqf_layout_sorted(t, q, r, fps) == 0
+    ns = O.sqf_num_slots(q)
+    probe = np.concatenate([fps, np.arange(0, 1 << (q + r), 7, dtype=np.uint32)])
+    want = _oracle_fp_lookup(t, q, r, probe)
+    assert (want[: fps.size] != 0xFFFFFFFF).all()
+    assert np.array_equal(run_driver(driver, tmp_path, t, q, r, probe, mirror=True), want)
+    assert ns > 700
