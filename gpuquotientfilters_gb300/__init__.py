@@ -46,7 +46,8 @@ class gqf_sqf_job(C.Structure):
 
 
 class gqf_batch_tuning(C.Structure):
-    _fields_ = [("bucket_bits", C.c_int), ("scatter_chunk", C.c_int)]
+    _fields_ = [("bucket_bits", C.c_int), ("scatter_chunk", C.c_int), ("cta_threads", C.c_int),
+                ("items_per_thread", C.c_int)]
 
 
 class gqf_server_config(C.Structure):
@@ -410,15 +411,20 @@ def filter_from_image(img: bytes) -> quotient_filter:
 
 
 # ------------------------------------------------------------ batched filters
+BATCH_DIRECT, BATCH_GRAPH, BATCH_PERSISTENT = 0, 1, 2
+
+
 class Batch:
-    """Many filters built and queried by one launch per pipeline kernel,
-    replayed from a captured CUDA graph (gqf_batch_* in include/gqf.h).
+    """Many filters built and queried together (gqf_batch_* in
+    include/gqf.h): by one launch per pipeline kernel, replayed from a
+    captured CUDA graph, or by one persistent cooperative kernel.
 
     jobs: sequence of (filter, build_keys or None, lookup_keys or None,
     results or None); tensors or raw device pointers with lengths taken from
     the tensors (pass (ptr, n) tuples for raw pointers)."""
 
-    def __init__(self, jobs, no_duplicates=True, bucket_bits=0, scatter_chunk=0):
+    def __init__(self, jobs, no_duplicates=True, bucket_bits=0, scatter_chunk=0, cta_threads=0,
+                 items_per_thread=0):
         def ptr_len(x):
             if x is None:
                 return 0, 0
@@ -432,22 +438,24 @@ class Batch:
             lp, ln = ptr_len(lk)
             rp, _ = ptr_len(res)
             arr[i] = gqf_sqf_job(qf, bn, bp, ln, lp, rp)
-        tune = gqf_batch_tuning(int(bucket_bits), int(scatter_chunk))
+        tune = gqf_batch_tuning(int(bucket_bits), int(scatter_chunk), int(cta_threads), int(items_per_thread))
         h = C.c_void_p()
         _check(_lib().gqf_batch_create(C.byref(h), arr, len(jobs), int(bool(no_duplicates)), C.byref(tune)),
                "gqf_batch_create")
         self._h = h
 
-    def run(self, use_graph=True, stream=None) -> float:
+    def run(self, use_graph=True, stream=None, persistent=False) -> float:
+        """Runs the batch once and returns its device time in ms."""
+        mode = BATCH_PERSISTENT if persistent else (BATCH_GRAPH if use_graph else BATCH_DIRECT)
         ms = C.c_float(0.0)
-        _check(_lib().gqf_batch_run(self._h, int(bool(use_graph)), _stream_ptr(stream), C.byref(ms)),
-               "gqf_batch_run")
+        _check(_lib().gqf_batch_run(self._h, mode, _stream_ptr(stream), C.byref(ms)), "gqf_batch_run")
         return ms.value
 
     def tuning(self):
         t = gqf_batch_tuning()
         _check(_lib().gqf_batch_tuning_of(self._h, C.byref(t)), "gqf_batch_tuning_of")
-        return {"bucket_bits": t.bucket_bits, "scatter_chunk": t.scatter_chunk}
+        return {"bucket_bits": t.bucket_bits, "scatter_chunk": t.scatter_chunk, "cta_threads": t.cta_threads,
+                "items_per_thread": t.items_per_thread}
 
     def close(self):
         if getattr(self, "_h", None):

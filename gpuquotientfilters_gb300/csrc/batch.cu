@@ -9,67 +9,17 @@
 //
 // Per filter the results are exactly those of bulkBuildSegmentedLayouts and
 // launchUnsortedLookups on the same inputs (same kernels' per-bucket and
-// per-query code; only the work lists differ).
+// per-query code; only the work lists differ).  The same pipeline also runs
+// as one persistent cooperative launch (batch_persist.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
+#include "batch.cuh"
 #include "host_common.cuh"
-#include "sqf_build.cuh"
-#include "sqf_lookup.cuh"
 
 namespace gqf {
-
-struct MfFilter {
-    uint8_t *table;
-    const uint32_t *keys;     // bulk build input (n_keys; 0 = no build)
-    const uint32_t *queries;  // lookups (n_q)
-    uint32_t *results;
-    uint32_t q, r, nslots, T;
-    uint32_t n_keys, n_q;
-    uint32_t chunk0, bucket0, qchunk0, fix0;  // first work unit of each list
-    uint32_t nb, fix_cap;
-};
-
-struct MfParams {
-    const MfFilter *f;
-    uint32_t nf;
-    uint32_t tb, cap_items;
-    int nodup, bitmap_ok;
-    uint32_t *bcnt, *bbase, *bfill;  // per global bucket
-    uint32_t *items;                 // bucketed fingerprints of all filters
-    unsigned long long *status;      // look-back descriptors, per global bucket
-    uint32_t *ticket;
-    uint32_t *fix_list, *fix_cnt;    // per-filter regions / counters
-    uint32_t *err;
-    uint32_t total_buckets;
-};
-
-// filter owning work unit x of a list whose per-filter starts are field F
-template <uint32_t MfFilter::*F>
-__device__ __forceinline__ uint32_t mf_owner(const MfFilter *f, uint32_t nf, uint32_t x)
-{
-    uint32_t lo = 0, hi = nf;  // last filter with start <= x
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (f[mid].*F <= x) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ BucketGeom mf_geom(const MfFilter &f, uint32_t tb)
-{
-    BucketGeom g;
-    g.q = f.q;
-    g.r = f.r;
-    g.tb = tb;
-    g.nb = f.nb;
-    g.shift = f.r + tb;
-    g.fp_mask = (f.q + f.r >= 32) ? 0xFFFFFFFFu : ((1u << (f.q + f.r)) - 1u);
-    return g;
-}
 
 // Slots past the last bucket's quotients only receive spill: clear them in
 // every filter that is rebuilt (the single-filter path does this with a
@@ -173,6 +123,7 @@ __global__ void __launch_bounds__(THREADS, (THREADS >= 1024 ? 1 : 2)) k_mf_layou
     a.fix_list = p.fix_list + f.fix0;
     a.fix_cnt = p.fix_cnt + fi;
     a.fix_cap = f.fix_cap;
+    a.fix_soft = 1;
     a.err = p.err;
     bucket_layout_body<THREADS, QPT, BPE>(a, s_gb - f.bucket0);
 }
@@ -182,16 +133,12 @@ __global__ void k_mf_fixup(MfParams p)
 {
     for (uint32_t fi = blockIdx.x; fi < p.nf; fi += gridDim.x) {
         const MfFilter &f = p.f[fi];
-        if (!f.n_keys) continue;
-        const uint32_t nf = min(p.fix_cnt[fi], f.fix_cap);
-        for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x)
-            f.table[(size_t)p.fix_list[f.fix0 + i] * BPE + (BPE - 1)] |= 4u;
+        if (f.n_keys) mf_occupied_bits<BPE>(p, f, fi, threadIdx.x, blockDim.x);
     }
 }
 
 // Lookups of all filters: work unit = MF_QCHUNK queries of one filter, each
 // thread answering LOOKUP_QPT of them as k_lookup_unsorted does.
-constexpr uint32_t MF_QCHUNK = LOOKUP_THREADS * LOOKUP_QPT;
 template <int BPE>
 __global__ void __launch_bounds__(LOOKUP_THREADS) k_mf_lookup(MfParams p, uint32_t total)
 {
@@ -235,6 +182,12 @@ struct Batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the persistent pipeline (one cooperative launch); pkernel == nullptr
+    // when the tuning's shape is not one of the compiled ones
+    MfPersist px{};
+    const void *pkernel = nullptr;
+    int pthreads = 0, pgrid = 0;
+    size_t psmem = 0;
 };
 
 template <typename K>
@@ -333,12 +286,18 @@ static int mf_create(Batch *b, const gqf_sqf_job *jobs, int count, int no_duplic
     b->tune.scatter_chunk = tune && tune->scatter_chunk ? tune->scatter_chunk : 8192;
     if (b->tune.scatter_chunk != 2048 && b->tune.scatter_chunk != 8192 && b->tune.scatter_chunk != 32768)
         return GQF_ERR_ARG;
+    b->tune.cta_threads = tune && tune->cta_threads ? tune->cta_threads : 256;
+    b->tune.items_per_thread = tune && tune->items_per_thread ? tune->items_per_thread : 32;
+    if ((b->tune.cta_threads != 128 && b->tune.cta_threads != 256) ||
+        (b->tune.items_per_thread != 8 && b->tune.items_per_thread != 32))
+        return GQF_ERR_ARG;
     uint32_t tb = (uint32_t)std::min<int>(std::max(b->tune.bucket_bits, 10), 13);
     if (qmin < 32 && qmin < tb) return GQF_ERR_ARG;  // every rebuilt filter spans whole buckets
     b->tune.bucket_bits = (int)tb;
     // work lists
     std::vector<MfFilter> hf(count);
-    uint32_t chunks = 0, buckets = 0, qchunks = 0, fix0 = 0;
+    uint32_t chunks = 0, buckets = 0, qchunks = 0, fix0 = 0, pchunks = 0;
+    const uint32_t pchunk = (uint32_t)b->tune.cta_threads * (uint32_t)b->tune.items_per_thread;
     double max_avg = 0;
     for (int i = 0; i < count; i++) {
         const gqf_sqf &f = jobs[i].filter;
@@ -354,12 +313,14 @@ static int mf_create(Batch *b, const gqf_sqf_job *jobs, int count, int no_duplic
         m.n_keys = (uint32_t)jobs[i].n_build;
         m.n_q = (uint32_t)jobs[i].n_lookup;
         m.chunk0 = chunks;
+        m.pchunk0 = pchunks;
         m.bucket0 = buckets;
         m.qchunk0 = qchunks;
         m.fix0 = fix0;
         m.nb = m.n_keys ? 1u << (f.qbits - tb) : 0u;
         m.fix_cap = m.n_keys ? std::max<uint32_t>(1024u, m.nslots / 8) : 0u;
         chunks += (m.n_keys + b->tune.scatter_chunk - 1) / b->tune.scatter_chunk;
+        pchunks += (m.n_keys + pchunk - 1) / pchunk;
         buckets += m.nb;
         qchunks += (m.n_q + MF_QCHUNK - 1) / MF_QCHUNK;
         fix0 += m.fix_cap;
@@ -396,6 +357,7 @@ static int mf_create(Batch *b, const gqf_sqf_job *jobs, int count, int no_duplic
     z.take<uint32_t>(1);                                 // ticket
     z.take<uint32_t>(count);                             // fix_cnt
     z.take<uint32_t>(1);                                 // err
+    z.take<uint32_t>(4);                                 // grid barrier of the persistent pipeline
     const size_t ctrl1 = z.off;
     z.take<uint32_t>(std::max(buckets, 1u));             // bbase
     z.take<uint32_t>(std::max<uint64_t>(n_items, 1));    // items
@@ -409,6 +371,7 @@ static int mf_create(Batch *b, const gqf_sqf_job *jobs, int count, int no_duplic
     b->p.ticket = c.take<uint32_t>(1);
     b->p.fix_cnt = c.take<uint32_t>(count);
     b->p.err = c.take<uint32_t>(1);
+    b->px.bar = c.take<uint32_t>(4);
     b->p.bbase = c.take<uint32_t>(std::max(buckets, 1u));
     b->p.items = c.take<uint32_t>(std::max<uint64_t>(n_items, 1));
     b->p.fix_list = c.take<uint32_t>(std::max<uint64_t>(fix_total, 1));
@@ -431,6 +394,32 @@ static int mf_create(Batch *b, const gqf_sqf_job *jobs, int count, int no_duplic
         GQF_CK(mf_with_layout<1>(tb, [&](auto klay, int) { return mf_smem(klay, b->layout_smem); }));
     else
         GQF_CK(mf_with_layout<2>(tb, [&](auto klay, int) { return mf_smem(klay, b->layout_smem); }));
+    // the persistent shape: quotients per layout thread = 2^tb / threads
+    b->px.total_chunks = pchunks;
+    b->px.total_buckets = buckets;
+    b->px.total_qchunks = qchunks;
+    b->px.any_build = b->any_build ? 1 : 0;
+    b->px.any_lookup = b->any_lookup ? 1 : 0;
+    {
+        const int threads = b->tune.cta_threads, ipt = b->tune.items_per_thread, qpt = (1 << tb) / threads;
+        const size_t sm = std::max({(size_t)b->nbmax * 4, (size_t)pchunk * 4 + (size_t)b->nbmax * 8, b->layout_smem});
+        auto setup = [&](const void *kern, int t) -> cudaError_t {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, t, sm);
+            if (e != cudaSuccess) return e;
+            if (per_sm > 0) {
+                b->pkernel = kern;
+                b->pthreads = t;
+                b->pgrid = per_sm * di.sms;
+                b->psmem = sm;
+            }
+            return cudaSuccess;
+        };
+        const void *kern = mf_persistent_kernel((int)b->bpe, threads, ipt, qpt);
+        if (kern) GQF_CK(setup(kern, threads));
+    }
     GQF_CK(cudaEventCreate(&b->ev0));
     GQF_CK(cudaEventCreate(&b->ev1));
     GQF_CK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
@@ -474,8 +463,14 @@ int gqf_batch_run(gqf_batch *batch, int use_graph, void *stream, float *ms)
     Batch *b = reinterpret_cast<Batch *>(batch);
     if (!b) return GQF_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (use_graph == GQF_BATCH_PERSISTENT && !b->pkernel) return GQF_ERR_ARG;
     if (ms) GQF_CK(cudaEventRecord(b->ev0, s));
-    if (use_graph) {
+    if (use_graph == GQF_BATCH_PERSISTENT) {
+        GQF_CK(cudaMemsetAsync(b->ctrl, 0, b->ctrl_bytes, s));
+        void *args[] = {&b->p, &b->px};
+        GQF_CK(cudaLaunchCooperativeKernel(b->pkernel, dim3(b->pgrid), dim3(b->pthreads), args, b->psmem, s));
+        count_launches(1);
+    } else if (use_graph) {
         GQF_CK(cudaGraphLaunch(b->exec, s));
         count_launches(1);
     } else {

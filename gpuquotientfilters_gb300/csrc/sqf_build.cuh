@@ -454,6 +454,10 @@ struct LayoutArgs {
     uint32_t *fix_list;
     uint32_t *fix_cnt;
     uint32_t fix_cap;
+    // Fix-ups past fix_cap: an error (0), or dropped (1) because the caller
+    // repairs the filter's occupied bits from its items when *fix_cnt ends
+    // above fix_cap (batched builds).
+    int fix_soft = 0;
     uint32_t *err;
     // In-place update (insert / delete, one-byte slots, bitmap mode): A is
     // decoded bucket by bucket from this snapshot of the table taken before
@@ -996,7 +1000,7 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
         } else {
             uint32_t gp = atomicAdd(a.fix_cnt, 1u);
             if (gp < a.fix_cap) a.fix_list[gp] = xa;
-            else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+            else if (!a.fix_soft) atomicOr(a.err, DEV_ERR_BUCKET_CAP);
         }
     };
     // E: emit elements; record occupied quotients (bit array) and the ones
@@ -1064,7 +1068,7 @@ __device__ __forceinline__ void bucket_layout_body(const LayoutArgs &a, const ui
         for (uint32_t i = tid; i < nf; i += THREADS) {
             uint32_t gp = s_fbase + i;
             if (gp < a.fix_cap) a.fix_list[gp] = s_fix[i];
-            else atomicOr(a.err, DEV_ERR_BUCKET_CAP);
+            else if (!a.fix_soft) atomicOr(a.err, DEV_ERR_BUCKET_CAP);
         }
     }
     // G: store the tile (occupied bits merged in): head bytes, 16-byte body,

@@ -288,10 +288,9 @@ __device__ __forceinline__ void bucket_insert_merge(const LayoutArgs &a, const u
         return;
     }
     const uint32_t pfirst = s_pfirst, pend = s_pend;
-    // this thread's stretches [s0, s1) and their fingerprints
+    // this thread's stretches, windows [win0, win1), and their fingerprints
     const uint32_t wpt = (NWIN + THREADS - 1) / THREADS;
     const uint32_t win0 = min(NWIN, tid * wpt), win1 = min(NWIN, win0 + wpt);
-    const uint32_t s0 = win0 * MERGE_WS, s1 = win1 * MERGE_WS;
     const uint32_t k0 = win0 < NWIN ? s_wbase[win0] : nbn;
     const uint32_t k1 = win1 < NWIN ? s_wbase[win1] : nbn;
     // order them by (insertion point, fingerprint) -- a handful per stretch --

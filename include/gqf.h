@@ -227,16 +227,28 @@ typedef struct gqf_sqf_job {
 } gqf_sqf_job;
 /* Launch shape of a batch (0 = default): bucket_bits = log2 quotients per
  * layout CTA (10..13, default 12); scatter_chunk = keys per scatter CTA
- * (2048, 8192 or 32768, default 8192). */
+ * (2048, 8192 or 32768, default 8192).  The persistent pipeline's shape:
+ * cta_threads (128 or 256, default 256) and items_per_thread (keys per
+ * thread of a scatter chunk: 8 or 32, default 32); its layout threads own
+ * 2^bucket_bits / cta_threads quotients each, 16 or 32 (other shapes leave
+ * the persistent mode unavailable: GQF_ERR_ARG from gqf_batch_run). */
 typedef struct gqf_batch_tuning {
     int bucket_bits;
     int scatter_chunk;
+    int cta_threads;
+    int items_per_thread;
 } gqf_batch_tuning;
 typedef struct gqf_batch gqf_batch;
 int gqf_batch_create(gqf_batch **out, const gqf_sqf_job *jobs, int count, int no_duplicates,
                      const gqf_batch_tuning *tuning);
-/* use_graph != 0: one cudaGraphLaunch of the captured pipeline; 0: the same
- * kernels launched directly on `stream` */
+/* use_graph: GQF_BATCH_DIRECT (0) launches the pipeline's kernels on
+ * `stream`; GQF_BATCH_GRAPH (1) replays them as one captured CUDA graph;
+ * GQF_BATCH_PERSISTENT (2) runs the whole pipeline as ONE cooperative
+ * kernel launch whose CTAs take work units from the same lists and meet at
+ * grid barriers between the phases (bounded waits: GQF_ERR_TIMEOUT). */
+#define GQF_BATCH_DIRECT 0
+#define GQF_BATCH_GRAPH 1
+#define GQF_BATCH_PERSISTENT 2
 int gqf_batch_run(gqf_batch *batch, int use_graph, void *stream, float *ms);
 int gqf_batch_tuning_of(const gqf_batch *batch, gqf_batch_tuning *out);
 int gqf_batch_destroy(gqf_batch *batch);

@@ -1,6 +1,7 @@
 """Batched filters (one launch per pipeline kernel for many filters, CUDA
-graph replay): every filter's table and lookup results are identical to the
-oracle's and to the single-filter API's, for every launch shape."""
+graph replay, or the whole pipeline as one persistent cooperative kernel):
+every filter's table and lookup results are identical to the oracle's and to
+the single-filter API's, for every launch shape."""
 import numpy as np
 import pytest
 
@@ -54,6 +55,75 @@ def test_batch_build_and_lookup(gqf, cuda, bucket_bits, chunk):
     b.close()
     for qf, *_ in jobs:
         G.freeFilterGPU(qf)
+
+
+def check_tables(G, jobs, want, look_want):
+    for (qf, dk, dl, res), t, lw in zip(jobs, want, look_want):
+        assert np.array_equal(G.table_bytes(qf), t)
+        if lw is not None:
+            assert np.array_equal(from_dev(res)[: lw.size], lw)
+
+
+# nearly full filters included: (13, 0.95) and, with duplicates, more items than quotients
+SPEC_P = [(12, 0.5, 300), (13, 0.95, 5000), (12, 0.85, 0), (15, 0.6, 256), (16, 0.9, 7000), (14, 0.75, 1000),
+          (12, 0.9, 4096), (13, 0.5, 1)]
+
+
+@pytest.mark.parametrize("threads,ipt,bucket_bits", [(256, 32, 13), (256, 8, 12), (128, 32, 12), (128, 8, 11)])
+@pytest.mark.parametrize("nodup", [True, False])
+def test_batch_persistent(gqf, cuda, threads, ipt, bucket_bits, nodup):
+    """The whole pipeline as one cooperative launch: same tables and results
+    as the oracle, run after run, interleaved with the graph replay.  With
+    duplicates some filters hold more items than quotients, so most of their
+    buckets start in the previous bucket's spill and their occupied-bit
+    fix-up list overflows: the filter's bits are then set from its items."""
+    G, torch = gqf, cuda
+    spec = [s for s in SPEC_P if s[0] >= bucket_bits]
+    jobs, host = make_jobs(G, torch, spec, 8 + threads + ipt, nodup=nodup)
+    want, look_want = [], []
+    for q, keys, look in host:
+        t = O.sqf_new(q, 5)
+        assert O.sqf_bulk_build(t, q, 5, keys, nodup) == 0
+        want.append(t)
+        look_want.append(O.sqf_lookup(t, q, 5, look) if look.size else None)
+    b = G.Batch(jobs, nodup, bucket_bits, 0, threads, ipt)
+    assert b.tuning()["cta_threads"] == threads and b.tuning()["items_per_thread"] == ipt
+    for persistent in (True, False, True):
+        b.run(True, persistent=persistent)
+        check_tables(G, jobs, want, look_want)
+    b.close()
+    for qf, *_ in jobs:
+        G.freeFilterGPU(qf)
+
+
+def test_batch_persistent_r13_and_lookup_only(gqf, cuda):
+    G, torch = gqf, cuda
+    spec = [(13, 0.7, 2000), (14, 0.8, 3000), (12, 0.6, 0)]
+    jobs, host = make_jobs(G, torch, spec, 9, r=13)
+    G.Batch(jobs, True).run(persistent=True)
+    check(G, torch, jobs, host, r=13)
+    jobs2 = [(qf, None, dl, torch.empty(max(1, dl.numel() if dl is not None else 1), dtype=torch.int32,
+                                        device="cuda") if dl is not None else None)
+             for (qf, dk, dl, res) in jobs]
+    G.Batch(jobs2, True).run(persistent=True)
+    for (qf, _, dl, res2), (q, keys, look) in zip(jobs2, host):
+        if look.size:
+            t = O.sqf_new(q, 13)
+            O.sqf_bulk_build(t, q, 13, keys, True)
+            assert np.array_equal(from_dev(res2)[: look.size], O.sqf_lookup(t, q, 13, look))
+
+
+def test_batch_persistent_shape_not_compiled(gqf, cuda):
+    """A shape whose layout threads would own 64 quotients has no persistent
+    kernel: the graph replay still runs, the persistent mode is refused."""
+    G, torch = gqf, cuda
+    jobs, host = make_jobs(G, torch, [(14, 0.6, 500)], 10)
+    b = G.Batch(jobs, True, 13, 0, 128, 32)
+    b.run(True)
+    check(G, torch, jobs, host)
+    with pytest.raises(G.GQFError):
+        b.run(True, persistent=True)
+    b.close()
 
 
 def test_batch_equals_single_filter_api(gqf, cuda):

@@ -63,8 +63,11 @@ def test_batch_class_and_candidates():
     assert cls.startswith("r5:q12-16:")
     assert A.batch_class([(14, 0)], 5) == "r5:lookups-only"
     cands = A.candidates(shapes)
-    assert all(bb <= 12 for bb, _ in cands)  # every rebuilt filter spans whole buckets
-    assert {ch for _, ch in cands} == set(A.SCATTER_CHUNKS)
+    assert all(c[1] <= 12 for c in cands)  # every rebuilt filter spans whole buckets
+    assert {c[2] for c in cands if c[0] == "graph"} == set(A.SCATTER_CHUNKS)
+    pers = [c for c in cands if c[0] == "persistent"]
+    assert {(c[2], c[3]) for c in pers} == {(t, i) for t in A.CTA_THREADS for i in A.ITEMS_PER_THREAD}
+    assert all((1 << c[1]) // c[2] in A.QUOTIENTS_PER_THREAD for c in pers)
 
 
 class _FakeQF:
@@ -76,11 +79,13 @@ class _FakeBatch:
     """Stands in for G.Batch: run() returns a time that depends on the shape."""
     calls = []
 
-    def __init__(self, jobs, no_duplicates, bb, ch):
-        self.bb, self.ch = bb, ch
-        _FakeBatch.calls.append((bb, ch))
+    def __init__(self, jobs, no_duplicates, bb, ch, threads=0, ipt=0):
+        self.bb, self.ch, self.threads, self.ipt = bb, ch, threads, ipt
+        _FakeBatch.calls.append((bb, ch, threads, ipt))
 
-    def run(self, use_graph=True, stream=None):
+    def run(self, use_graph=True, stream=None, persistent=False):
+        if persistent:  # the persistent form wins at 256 threads x 32 keys, 12 bucket bits
+            return 0.5 + abs(self.bb - 12) + (0.0 if (self.threads, self.ipt) == (256, 32) else 0.3)
         return 1.0 + abs(self.bb - 11) + (0.0 if self.ch == 8192 else 0.5)
 
     def close(self):
@@ -96,7 +101,8 @@ def test_tune_picks_fastest_and_caches(tmp_path):
     jobs = [(_FakeQF(13), (0, 40000), None, None), (_FakeQF(15), (0, 90000), None, None)]
     _FakeBatch.calls = []
     choice, times = A.tune(_FakeG, jobs, cache=cache)
-    assert choice == {"bucket_bits": 11, "scatter_chunk": 8192}
+    assert choice == {"mode": "persistent", "bucket_bits": 12, "scatter_chunk": 0, "cta_threads": 256,
+                      "items_per_thread": 32}
     assert len(times) == len(A.candidates([(13, 40000), (15, 90000)]))
     table = json.load(open(cache))
     assert list(table.values())[0]["best"] == choice
