@@ -6,9 +6,10 @@ lookups, 2^24 sorted lookups (50% inserted keys, 50% fresh draws), an
 insert of 2^20 fresh keys and 2^20 deletes of present keys.  `value` is the
 step's operations (keys built + queries + inserts + deletes) per second of
 device time, summed over ranks (each rank runs an independent filter:
-replicas, weak scaling).  Every op is timed on its stream with CUDA events,
-with L2 flushed before each op.  `e2e` repeats the step through the same API
-from pinned host buffers, host<->device copies inside the timed region.
+replicas, weak scaling).  Every op is a synchronous call (it returns its
+status) timed on its stream with CUDA events, with L2 flushed before each
+op.  `e2e` repeats the step through the same API from pinned host buffers,
+host<->device copies inside the timed region, the ops queued asynchronously.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -482,8 +483,10 @@ def e2e_step(args, G, torch, dev, stream, c, qf):
     would run them: a step's inputs go up on the copy stream (double-buffered,
     so the next step's inputs load while this step computes), each op waits
     only for its own input, and each lookup's results come back on a third
-    stream while the later ops run.  The timed region runs from before the
-    first copy to after the last result is on the host."""
+    stream while the later ops run.  The ops are queued asynchronously
+    (sync=False: the C ABI with no timing pointer), so the host runs ahead of
+    the device.  The timed region runs from before the first copy to after
+    the last result is on the host."""
     def pinned(a):
         return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).pin_memory()
 
@@ -523,12 +526,12 @@ def e2e_step(args, G, torch, dev, stream, c, qf):
         b, ev = bufs[step % 2], pending.pop(step)
         lu, ls = torch.cuda.Event(), torch.cuda.Event()
         stream.wait_event(ev["keys"])
-        G.bulkBuildSegmentedLayouts(qf, N_KEYS, b["keys"], True, stream=stream)
+        G.bulkBuildSegmentedLayouts(qf, N_KEYS, b["keys"], True, stream=stream, sync=False)
         stream.wait_event(ev["look"])
         stream.wait_event(b["fetched"])
-        G.launchUnsortedLookups(qf, N_LOOKUP, b["look"], b["out"], stream=stream)
+        G.launchUnsortedLookups(qf, N_LOOKUP, b["look"], b["out"], stream=stream, sync=False)
         lu.record(stream)
-        G.launchSortedLookups(qf, N_LOOKUP, b["look"], b["out2"], stream=stream)
+        G.launchSortedLookups(qf, N_LOOKUP, b["look"], b["out2"], stream=stream, sync=False)
         ls.record(stream)
         down.wait_event(lu)
         with torch.cuda.stream(down):
@@ -537,9 +540,9 @@ def e2e_step(args, G, torch, dev, stream, c, qf):
             h_out2.copy_(b["out2"], non_blocking=True)
             b["fetched"].record(down)
         stream.wait_event(ev["ins"])
-        G.insert(qf, N_INSERT, b["ins"], stream=stream)
+        G.insert(qf, N_INSERT, b["ins"], stream=stream, sync=False)
         stream.wait_event(ev["del"])
-        G.superclusterDeletes(qf, N_DELETE, b["del"], stream=stream)
+        G.superclusterDeletes(qf, N_DELETE, b["del"], stream=stream, sync=False)
         b["free"].record(stream)
 
     def steps(n):
@@ -559,6 +562,7 @@ def e2e_step(args, G, torch, dev, stream, c, qf):
     stream.wait_event(bufs[(args.steps - 1) % 2]["fetched"])
     ev1.record(stream)
     ev1.synchronize()
+    G.stream_status(stream)  # a device-side error of any queued op fails the run
     ms = ev0.elapsed_time(ev1) / args.steps
     ops = N_KEYS + 2 * N_LOOKUP + N_INSERT + N_DELETE
     return {"value": ops / ms / 1e3, "unit": "M ops/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,

@@ -173,11 +173,24 @@ def _check(st: int, what: str):
         raise GQFError(st, what)
 
 
-def _timed(fn, *args, stream=None):
+def _timed(fn, *args, stream=None, sync=True):
+    """Calls a C ABI op.  sync=True: the call waits for the op and returns
+    its device time in ms (a device-side error is its status).  sync=False:
+    the op is only queued on `stream` and None is returned; a deferred
+    device-side error shows in gqf_stream_status / stream_status()."""
+    if not sync:
+        _check(fn(*args, _stream_ptr(stream), None), fn.__name__)
+        return None
     ms = C.c_float(0.0)
     st = fn(*args, _stream_ptr(stream), C.byref(ms))
     _check(st, fn.__name__)
     return ms.value
+
+
+def stream_status(stream=None) -> None:
+    """Waits for `stream` and raises GQFError if an op queued on it with
+    sync=False hit a device-side error (gqf_stream_status)."""
+    _check(_lib().gqf_stream_status(_stream_ptr(stream)), "gqf_stream_status")
 
 
 # ------------------------------------------------------------- host helpers
@@ -220,9 +233,9 @@ def freeFilterGPU(qf: quotient_filter) -> None:
     _check(_lib().gqf_sqf_free(C.byref(qf)), "freeFilterGPU")
 
 
-def bulkBuildSegmentedLayouts(qf, numValues, d_insertValues, NoDuplicates, stream=None) -> float:
+def bulkBuildSegmentedLayouts(qf, numValues, d_insertValues, NoDuplicates, stream=None, sync=True):
     return _timed(_lib().gqf_sqf_bulk_build, C.byref(qf), int(numValues), _ptr(d_insertValues),
-                  int(bool(NoDuplicates)), stream=stream)
+                  int(bool(NoDuplicates)), stream=stream, sync=sync)
 
 
 # The reference's other two bulk builds produce the same (canonical) table.
@@ -230,32 +243,32 @@ bulkBuildParallelMerging = bulkBuildSegmentedLayouts
 bulkBuildSequentialShifts = bulkBuildSegmentedLayouts
 
 
-def launchUnsortedLookups(qf, numValues, d_lookupValues, d_returnValues, stream=None) -> float:
+def launchUnsortedLookups(qf, numValues, d_lookupValues, d_returnValues, stream=None, sync=True):
     return _timed(_lib().gqf_sqf_lookup_unsorted, C.byref(qf), int(numValues), _ptr(d_lookupValues),
-                  _ptr(d_returnValues), stream=stream)
+                  _ptr(d_returnValues), stream=stream, sync=sync)
 
 
-def launchSortedLookups(qf, numValues, d_lookupValues, d_returnValues, stream=None) -> float:
+def launchSortedLookups(qf, numValues, d_lookupValues, d_returnValues, stream=None, sync=True):
     return _timed(_lib().gqf_sqf_lookup_sorted, C.byref(qf), int(numValues), _ptr(d_lookupValues),
-                  _ptr(d_returnValues), stream=stream)
+                  _ptr(d_returnValues), stream=stream, sync=sync)
 
 
-def insert(qf, numValues, d_insertValues, stream=None) -> float:
-    return _timed(_lib().gqf_sqf_insert, C.byref(qf), int(numValues), _ptr(d_insertValues), stream=stream)
+def insert(qf, numValues, d_insertValues, stream=None, sync=True):
+    return _timed(_lib().gqf_sqf_insert, C.byref(qf), int(numValues), _ptr(d_insertValues), stream=stream, sync=sync)
 
 
-def superclusterDeletes(qf, numValues, d_deleteValues, stream=None) -> float:
-    return _timed(_lib().gqf_sqf_delete, C.byref(qf), int(numValues), _ptr(d_deleteValues), stream=stream)
+def superclusterDeletes(qf, numValues, d_deleteValues, stream=None, sync=True):
+    return _timed(_lib().gqf_sqf_delete, C.byref(qf), int(numValues), _ptr(d_deleteValues), stream=stream, sync=sync)
 
 
 def insertViaMerge(qf, d_insertedValues, numOldValues, d_newValues, numNewValues, NoDuplicates,
-                   stream=None) -> float:
+                   stream=None, sync=True):
     return _timed(_lib().gqf_sqf_insert_via_merge, C.byref(qf), _ptr(d_insertedValues), int(numOldValues),
-                  _ptr(d_newValues), int(numNewValues), int(bool(NoDuplicates)), stream=stream)
+                  _ptr(d_newValues), int(numNewValues), int(bool(NoDuplicates)), stream=stream, sync=sync)
 
 
-def mergeTwoFilters(qf1, qf2, NoDuplicates, stream=None) -> float:
-    return _timed(_lib().gqf_sqf_merge, C.byref(qf1), C.byref(qf2), int(bool(NoDuplicates)), stream=stream)
+def mergeTwoFilters(qf1, qf2, NoDuplicates, stream=None, sync=True):
+    return _timed(_lib().gqf_sqf_merge, C.byref(qf1), C.byref(qf2), int(bool(NoDuplicates)), stream=stream, sync=sync)
 
 
 def table_bytes(qf):
@@ -347,19 +360,19 @@ def freeCQFGPU(cqf) -> None:
     _check(_rsqf(cqf, "free")(C.byref(cqf)), "freeCQFGPU")
 
 
-def insertGPU(cqf, numValues, d_insertValues, d_returnValues, stream=None) -> float:
+def insertGPU(cqf, numValues, d_insertValues, d_returnValues, stream=None, sync=True):
     return _timed(_rsqf(cqf, "insert"), C.byref(cqf), int(numValues), _ptr(d_insertValues),
-                  _ptr(d_returnValues), stream=stream)
+                  _ptr(d_returnValues), stream=stream, sync=sync)
 
 
-def launchLookups(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None) -> float:
+def launchLookups(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None, sync=True):
     return _timed(_rsqf(cqf, "lookup_sorted"), C.byref(cqf), int(numValues), _ptr(d_lookupValues),
-                  _ptr(d_slotValuesArray), stream=stream)
+                  _ptr(d_slotValuesArray), stream=stream, sync=sync)
 
 
-def launchUnsortedLookupsRSQF(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None) -> float:
+def launchUnsortedLookupsRSQF(cqf, numValues, d_lookupValues, d_slotValuesArray, stream=None, sync=True):
     return _timed(_rsqf(cqf, "lookup_unsorted"), C.byref(cqf), int(numValues), _ptr(d_lookupValues),
-                  _ptr(d_slotValuesArray), stream=stream)
+                  _ptr(d_slotValuesArray), stream=stream, sync=sync)
 
 
 def rsqf_blocks_bytes(cqf):

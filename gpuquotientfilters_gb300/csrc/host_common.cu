@@ -72,6 +72,7 @@ int release_arena(int dev, cudaStream_t s)
     if (a->ptr) GQF_CK(cudaFreeAsync(a->ptr, s));
     GQF_CK(cudaStreamSynchronize(s));
     if (a->latch) GQF_CK(cudaFree(a->latch));
+    if (a->report) GQF_CK(cudaFreeHost(const_cast<uint32_t *>(a->report)));
     if (a->ev0) cudaEventDestroy(a->ev0);
     if (a->ev1) cudaEventDestroy(a->ev1);
     return GQF_OK;
@@ -85,6 +86,12 @@ void *arena_reserve(Arena &a, size_t bytes)
         if (cudaMemset(p, 0, 2 * sizeof(uint32_t)) != cudaSuccess) return nullptr;
         a.latch = p;
         a.err = p + 1;
+        uint32_t *h = nullptr;
+        if (cudaHostAlloc(reinterpret_cast<void **>(&h), 2 * sizeof(uint32_t), cudaHostAllocMapped) != cudaSuccess)
+            return nullptr;
+        h[0] = h[1] = 0;
+        if (cudaHostGetDevicePointer(reinterpret_cast<void **>(&a.report_dev), h, 0) != cudaSuccess) return nullptr;
+        a.report = h;
         cudaEventCreate(&a.ev0);
         cudaEventCreate(&a.ev1);
     }
@@ -126,6 +133,25 @@ __global__ void k_latch(uint32_t *latch, const uint32_t *err)
     if (*err) atomicOr(latch, *err);
 }
 
+__global__ void k_report(const uint32_t *err, const uint32_t *extra, uint32_t *host)
+{
+    host[0] = *err;
+    host[1] = extra ? *extra : 0u;
+    __threadfence_system();
+}
+
+int call_report(Arena &a, cudaStream_t s, const uint32_t *extra, uint32_t out[2])
+{
+    k_report<<<1, 1, 0, s>>>(a.err, extra, a.report_dev);
+    count_launches(1);
+    GQF_CK(cudaGetLastError());
+    GQF_CK(cudaEventRecord(a.ev1, s));
+    GQF_CK(cudaEventSynchronize(a.ev1));
+    out[0] = a.report[0];
+    out[1] = a.report[1];
+    return GQF_OK;
+}
+
 int call_end(Arena &a, cudaStream_t s, float *ms)
 {
     GQF_CK(cudaGetLastError());
@@ -135,12 +161,11 @@ int call_end(Arena &a, cudaStream_t s, float *ms)
         GQF_CK(cudaGetLastError());
         return GQF_OK;
     }
-    GQF_CK(cudaEventRecord(a.ev1, s));
-    GQF_CK(cudaEventSynchronize(a.ev1));
+    uint32_t rep[2];
+    int st = call_report(a, s, nullptr, rep);
+    if (st) return st;
     GQF_CK(cudaEventElapsedTime(ms, a.ev0, a.ev1));
-    uint32_t e = 0;
-    GQF_CK(cudaMemcpy(&e, a.err, sizeof(e), cudaMemcpyDeviceToHost));
-    return dev_err_to_status(e);
+    return dev_err_to_status(rep[0]);
 }
 
 }  // namespace gqf

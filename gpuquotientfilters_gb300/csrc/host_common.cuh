@@ -41,6 +41,11 @@ struct Arena {
     cudaStream_t stream = nullptr;
     uint32_t *latch = nullptr;  // persistent per-device error latch
     uint32_t *err = nullptr;    // per-call device error word
+    // two words of mapped pinned host memory: a synchronous call's error
+    // word (and one more flag) land here from the device, so the host reads
+    // them after the call's end event without a device-to-host copy
+    volatile uint32_t *report = nullptr;
+    uint32_t *report_dev = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
 };
@@ -85,6 +90,10 @@ int call_begin(Arena &a, cudaStream_t s, bool timed);
 // device error word to a status; otherwise ORs the error word into the
 // device latch for gqf_stream_status.
 int call_end(Arena &a, cudaStream_t s, float *ms);
+// Synchronous end of a step of a call: the device copies the error word
+// (and *extra, if given) into the arena's mapped host words, the host waits
+// for the stream and returns them in out[0], out[1].
+int call_report(Arena &a, cudaStream_t s, const uint32_t *extra, uint32_t out[2]);
 int dev_err_to_status(uint32_t e);
 
 int current_device();

@@ -465,11 +465,10 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
             if (st) return st;
             return call_end(ar, s, nullptr);
         }
-        GQF_CK(cudaEventRecord(ar.ev1, s));
-        GQF_CK(cudaEventSynchronize(ar.ev1));
-        uint32_t e = 0, fail = 0;
-        GQF_CK(cudaMemcpy(&e, ar.err, 4, cudaMemcpyDeviceToHost));
-        GQF_CK(cudaMemcpy(&fail, sc.fused_fail, 4, cudaMemcpyDeviceToHost));
+        uint32_t rep[2];
+        st = call_report(ar, s, sc.fused_fail, rep);
+        if (st) return st;
+        const uint32_t e = rep[0], fail = rep[1];
         GQF_CK(cudaEventElapsedTime(&ms_fused, ar.ev0, ar.ev1));
         if (!fail) {
             *ms = ms_fused;
@@ -509,10 +508,10 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
         if (st) return st;
         if (!ms) return call_end(ar, s, nullptr);
         // synchronous: look at the error word before deciding
-        GQF_CK(cudaEventRecord(ar.ev1, s));
-        GQF_CK(cudaEventSynchronize(ar.ev1));
-        uint32_t e = 0;
-        GQF_CK(cudaMemcpy(&e, ar.err, 4, cudaMemcpyDeviceToHost));
+        uint32_t rep[2];
+        st = call_report(ar, s, nullptr, rep);
+        if (st) return st;
+        const uint32_t e = rep[0];
         if ((e & DEV_ERR_BUCKET_OVER) && !exact) {
             exact = true;
             continue;

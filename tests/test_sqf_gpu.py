@@ -373,3 +373,32 @@ def test_skewed_bucket_set_semantics(gqf, cuda):
     f.delete(sel[:1000])
     O.sqf_delete(t, q, r, sel[:1000])
     assert_same_table(f, t)
+
+
+def test_python_async_calls(gqf, cuda):
+    """sync=False queues each op on the stream without waiting (the C ABI
+    with no timing pointer); stream_status() then reports any deferred
+    device-side error.  The results equal the synchronous calls' (oracle)."""
+    q, r = 16, 5
+    n = int(0.8 * (1 << q))
+    keys = O.mt_keys(91, n)
+    look = np.concatenate([keys[: n // 2], O.mt_keys(92, n // 2)])
+    ins, dels = O.mt_keys(93, 3000), keys[:2000].copy()
+    s = cuda.cuda.Stream()
+    qf = gqf.initFilterGPU(q, r)
+    try:
+        out = cuda.empty(look.size, dtype=cuda.int32, device="cuda")
+        dk, dl, di, dd = to_dev(cuda, keys), to_dev(cuda, look), to_dev(cuda, ins), to_dev(cuda, dels)
+        cuda.cuda.synchronize()
+        assert gqf.bulkBuildSegmentedLayouts(qf, keys.size, dk, True, stream=s, sync=False) is None
+        gqf.launchUnsortedLookups(qf, look.size, dl, out, stream=s, sync=False)
+        gqf.insert(qf, ins.size, di, stream=s, sync=False)
+        gqf.superclusterDeletes(qf, dels.size, dd, stream=s, sync=False)
+        gqf.stream_status(s)
+        t = oracle_build(q, r, keys)
+        assert np.array_equal(from_dev(out), O.sqf_lookup(t, q, r, look))
+        O.sqf_insert(t, q, r, ins)
+        O.sqf_delete(t, q, r, dels)
+        assert np.array_equal(gqf.table_bytes(qf), t)
+    finally:
+        gqf.freeFilterGPU(qf)
