@@ -223,11 +223,44 @@ static int extract_into(const uint8_t *table, uint32_t nslots, size_t nbytes, ui
 }
 
 // Hash + bucket the batch keys.  exact: histogram + device scan first.
+// Bucketing a batch: histogram + scan (exact bases) or speculative strides,
+// then the scatter.  Batches of up to SMALL_BATCH keys (inserts, deletes,
+// small builds) use 4096-key chunks so that enough CTAs share the work; the
+// large ones 32K-key chunks.
+constexpr uint32_t SMALL_BATCH = 1u << 22;
+constexpr int SMALL_THREADS = 256, SMALL_IPT = 16;
+
+template <int T, int IPT>
+static int bucket_batch_keys(const uint32_t *keys, uint32_t n, const LayoutPlan &p, Scratch &sc, bool exact,
+                             uint32_t *err, cudaStream_t s)
+{
+    const uint32_t grid = (n + T * IPT - 1) / (T * IPT);
+    if (exact) {
+        count_launches(2);
+        GQF_CK(set_smem(k_bucket_hist<T, IPT>, p.g.nb * 4));
+        k_bucket_hist<T, IPT><<<grid, T, p.g.nb * 4, s>>>(keys, n, p.g, sc.bcnt);
+        k_scan_bases<<<1, 1024, 0, s>>>(sc.bcnt, p.g.nb, sc.bbase);
+        GQF_CK(cudaMemsetAsync(sc.bcnt, 0, p.g.nb * 4, s));
+    }
+    count_launches(1);
+    auto kfn = k_hash_bucket<T, IPT, false>;
+    const size_t sm = (size_t)T * IPT * 4 + (size_t)p.g.nb * 8;
+    GQF_CK(set_smem(kfn, sm));
+    kfn<<<grid, T, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride, sc.bcnt,
+                            sc.bitems, nullptr, err);
+    GQF_CK(cudaGetLastError());
+    return GQF_OK;
+}
+
 static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, Scratch &sc, bool exact, bool pairs,
                         uint32_t *err, cudaStream_t s)
 {
     if (n == 0) return GQF_OK;
-    const uint32_t chunk = pairs ? PAIR_THREADS * PAIR_IPT : SCATTER_THREADS * SCATTER_IPT;
+    if (!pairs) {
+        return n <= SMALL_BATCH ? bucket_batch_keys<SMALL_THREADS, SMALL_IPT>(keys, n, p, sc, exact, err, s)
+                                : bucket_batch_keys<SCATTER_THREADS, SCATTER_IPT>(keys, n, p, sc, exact, err, s);
+    }
+    const uint32_t chunk = PAIR_THREADS * PAIR_IPT;
     const uint32_t grid = (n + chunk - 1) / chunk;
     const size_t sm = scatter_smem(p.g.nb, pairs);
     if (exact) {
@@ -239,17 +272,10 @@ static int bucket_batch(const uint32_t *keys, uint32_t n, const LayoutPlan &p, S
         GQF_CK(cudaMemsetAsync(sc.bcnt, 0, p.g.nb * 4, s));
     }
     count_launches(1);
-    if (pairs) {
-        auto kfn = k_hash_bucket<PAIR_THREADS, PAIR_IPT, true>;
-        GQF_CK(set_smem(kfn, sm));
-        kfn<<<grid, PAIR_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
-                                           sc.bcnt, sc.bitems, sc.bidx, err);
-    } else {
-        auto kfn = k_hash_bucket<SCATTER_THREADS, SCATTER_IPT, false>;
-        GQF_CK(set_smem(kfn, sm));
-        kfn<<<grid, SCATTER_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr,
-                                              exact ? 0xFFFFFFFFu : p.stride, sc.bcnt, sc.bitems, nullptr, err);
-    }
+    auto kfn = k_hash_bucket<PAIR_THREADS, PAIR_IPT, true>;
+    GQF_CK(set_smem(kfn, sm));
+    kfn<<<grid, PAIR_THREADS, sm, s>>>(keys, n, p.g, exact ? sc.bbase : nullptr, exact ? 0xFFFFFFFFu : p.stride,
+                                       sc.bcnt, sc.bitems, sc.bidx, err);
     GQF_CK(cudaGetLastError());
     return GQF_OK;
 }
