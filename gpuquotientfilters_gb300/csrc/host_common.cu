@@ -75,7 +75,23 @@ int release_arena(int dev, cudaStream_t s)
     if (a->report) GQF_CK(cudaFreeHost(const_cast<uint32_t *>(a->report)));
     if (a->ev0) cudaEventDestroy(a->ev0);
     if (a->ev1) cudaEventDestroy(a->ev1);
+    if (a->side) {
+        GQF_CK(cudaStreamSynchronize(a->side));
+        cudaStreamDestroy(a->side);
+        cudaEventDestroy(a->fork);
+        cudaEventDestroy(a->join);
+    }
     return GQF_OK;
+}
+
+cudaStream_t arena_side(Arena &a)
+{
+    if (!a.side) {
+        if (cudaStreamCreateWithFlags(&a.side, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+        if (cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        if (cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    }
+    return a.side;
 }
 
 void *arena_reserve(Arena &a, size_t bytes)

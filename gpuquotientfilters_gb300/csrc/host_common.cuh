@@ -47,8 +47,15 @@ struct Arena {
     volatile uint32_t *report = nullptr;
     uint32_t *report_dev = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // a side stream for work that can run beside the call's own kernels
+    // (the in-place updates' table snapshot), forked from and joined back
+    // into the call's stream by events
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::mutex mu;
 };
+// The side stream of the arena, created on first use (nullptr on failure).
+cudaStream_t arena_side(Arena &a);
 Arena &arena(int dev, cudaStream_t s);
 // Frees the arena of (dev, s) after the stream drains.
 int release_arena(int dev, cudaStream_t s);

@@ -462,14 +462,21 @@ static int rebuild(const gqf_sqf *qf, const gqf_sqf *qf2, const uint32_t *keys, 
         Scratch sc = carve(base, req_fused, false, &bytes);
         int st = call_begin(ar, s, ms != nullptr);
         if (st) return st;
+        // the snapshot is copied on the side stream while the batch is bucketed
+        cudaStream_t side = arena_side(ar);
+        if (!side) return GQF_ERR_CUDA;
+        GQF_CK(cudaEventRecord(ar.fork, s));
+        GQF_CK(cudaStreamWaitEvent(side, ar.fork, 0));
+        GQF_CK(cudaMemcpyAsync(sc.snap, qf->table, tg.T, cudaMemcpyDeviceToDevice, side));
+        GQF_CK(cudaEventRecord(ar.join, side));
         GQF_CK(cudaMemsetAsync(sc.bcnt, 0, sc.ctrl_bytes, s));
-        GQF_CK(cudaMemcpyAsync(sc.snap, qf->table, tg.T, cudaMemcpyDeviceToDevice, s));
         BucketSrc A{nullptr, nullptr, 0, nullptr}, B{nullptr, nullptr, 0, nullptr};
         if (n) {
             st = bucket_batch(keys, n, p, sc, true, false, ar.err, s);
             if (st) return st;
             B = BucketSrc{sc.bitems, sc.bbase, 0, sc.bcnt};
         }
+        GQF_CK(cudaStreamWaitEvent(s, ar.join, 0));
         st = launch_layout<BPE>(p, tg, qf->table, A, B, op, nodup, true, nullptr, sc, ar.err, s, sc.snap);
         if (st) return st;
         if (!ms) {
