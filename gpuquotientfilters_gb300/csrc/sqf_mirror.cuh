@@ -293,6 +293,8 @@ static __global__ void __launch_bounds__(MIR_BUILD_THREADS) k_sqf_mirror(TableVi
         return rem < MIR_TILE ? (uint32_t)rem : MIR_TILE;
     };
     uint32_t pend = 0;  // thread 0: stages with a copy in flight
+    // the table streams through L2 (evict first); the records stay (evict last)
+    const uint64_t pass = l2_policy_evict_first();
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -302,7 +304,7 @@ static __global__ void __launch_bounds__(MIR_BUILD_THREADS) k_sqf_mirror(TableVi
             const uint32_t b = t0 + j < t1 ? copy_bytes(t0 + j) : 0u;
             if (b) {
                 mbar_arrive_expect_tx(&bar[j], b);
-                bulk_g2s(mir_smem + j * MIR_TILE, v.t + (size_t)(t0 + j) * MIR_TILE, b, &bar[j]);
+                bulk_g2s_hint(mir_smem + j * MIR_TILE, v.t + (size_t)(t0 + j) * MIR_TILE, b, &bar[j], pass);
                 pend |= 1u << j;
             }
         }
@@ -338,7 +340,7 @@ static __global__ void __launch_bounds__(MIR_BUILD_THREADS) k_sqf_mirror(TableVi
             if (b2) {
                 fence_proxy_async_smem();
                 mbar_arrive_expect_tx(&bar[j], b2);
-                bulk_g2s(st, v.t + (size_t)(t + 2) * MIR_TILE, b2, &bar[j]);
+                bulk_g2s_hint(st, v.t + (size_t)(t + 2) * MIR_TILE, b2, &bar[j], pass);
                 pend |= 1u << j;
             }
         }
