@@ -124,12 +124,9 @@ QF_HD uint32_t mirror_query(uint32_t fq, uint32_t fr, uint32_t k, const uint32_t
     return ((eq >> f) & 1u) ? fq + f : GQF_NOT_FOUND;
 }
 
-#ifdef __CUDACC__
-// ---- build ---------------------------------------------------------------
-
 // 8x8 bit transpose of one table word: byte b of the result holds bit b of
 // the 8 slot bytes, slot i at bit i.
-__device__ __forceinline__ uint64_t bit_transpose8(uint64_t x)
+QF_HD uint64_t bit_transpose8(uint64_t x)
 {
     uint64_t t;
     t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
@@ -140,6 +137,75 @@ __device__ __forceinline__ uint64_t bit_transpose8(uint64_t x)
     x = x ^ t ^ (t << 28);
     return x;
 }
+
+// byte i of the result = byte (sel >> 4i) & 7 of the 8 bytes b:a (a low)
+QF_HD uint32_t byte_perm(uint32_t a, uint32_t b, uint32_t sel)
+{
+#ifdef __CUDA_ARCH__
+    return __byte_perm(a, b, sel);
+#else
+    const uint64_t ab = (uint64_t)a | ((uint64_t)b << 32);
+    uint32_t r = 0;
+    for (int i = 0; i < 4; i++) r |= (uint32_t)((ab >> (8 * ((sel >> (4 * i)) & 7u))) & 0xFFu) << (8 * i);
+    return r;
+#endif
+}
+
+// One build thread's 31 table words (248 slots) -> the record words (P bits
+// clear) of its 8 groups of 31 slots, and per group #occupied - #run starts.
+// Planes come per 32-slot chunk: four 8x8 bit transposes, then a 4x4 byte
+// transpose (byte b of plane word t = plane t of word b); group g (bits
+// [31g, 31g + 31) of the thread's slots) is cut from the chunk holding its
+// first slot and the next.  Gives exactly mirror_record's words.
+QF_HD void mirror_groups(const uint64_t *sw, uint32_t (&gp)[8][8], int (&cnt)[8])
+{
+    uint32_t prev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        uint32_t lo[4], hi[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int wi = 4 * c + j;
+            const uint64_t y = wi < (int)MIR_WORDS ? bit_transpose8(sw[wi]) : 0ull;
+            lo[j] = (uint32_t)y;
+            hi[j] = (uint32_t)(y >> 32);
+        }
+        uint32_t raw[8];  // bit b of the slot bytes: 0 shifted, 1 continuation, 2 occupied, 3.. remainder
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint32_t *x = h ? hi : lo;
+            const uint32_t ab01 = byte_perm(x[0], x[1], 0x5140), ab23 = byte_perm(x[0], x[1], 0x7362);
+            const uint32_t cd01 = byte_perm(x[2], x[3], 0x5140), cd23 = byte_perm(x[2], x[3], 0x7362);
+            raw[4 * h + 0] = byte_perm(ab01, cd01, 0x5410);
+            raw[4 * h + 1] = byte_perm(ab01, cd01, 0x7632);
+            raw[4 * h + 2] = byte_perm(ab23, cd23, 0x5410);
+            raw[4 * h + 3] = byte_perm(ab23, cd23, 0x7632);
+        }
+        uint32_t cur[8];
+        cur[0] = raw[2];
+        cur[1] = (raw[2] | raw[0]) & ~raw[1];
+        cur[2] = raw[1];
+#pragma unroll
+        for (int b = 0; b < 5; b++) cur[3 + b] = raw[3 + b];
+        // group g is complete once the chunk after the one holding its first slot is in
+        if (c >= 1) {
+#pragma unroll
+            for (int g = 0; g < 8; g++) {
+                if (((31 * g) >> 5) == c - 1) {
+                    const int off = (31 * g) & 31;
+#pragma unroll
+                    for (int w = 0; w < 8; w++) gp[g][w] = fshr32(prev[w], cur[w], (uint32_t)off) & 0x7FFFFFFFu;
+                    cnt[g] = popc32(gp[g][0]) - popc32(gp[g][1]);
+                }
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < 8; w++) prev[w] = cur[w];
+    }
+}
+
+#ifdef __CUDACC__
+// ---- build ---------------------------------------------------------------
 
 __device__ __forceinline__ uint64_t l2_policy_evict_last()
 {
@@ -186,54 +252,8 @@ __device__ __forceinline__ int mirror_tile(const uint8_t *st, int Dtile, uint32_
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint64_t *sw = reinterpret_cast<const uint64_t *>(st) + MIR_WORDS * tid;
     uint32_t gp[8][8];  // [group][record word]
-    uint32_t prev[8];
     int cnt[8];
-    // 32-slot chunks of planes: four transposed words, then a 4x4 byte
-    // transpose (byte b of plane word t = plane t of word b)
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-        uint32_t lo[4], hi[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int wi = 4 * c + j;
-            const uint64_t y = wi < (int)MIR_WORDS ? bit_transpose8(sw[wi]) : 0ull;
-            lo[j] = (uint32_t)y;
-            hi[j] = (uint32_t)(y >> 32);
-        }
-        uint32_t raw[8];  // bit b of the slot bytes: 0 shifted, 1 continuation, 2 occupied, 3.. remainder
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const uint32_t *x = h ? hi : lo;
-            const uint32_t ab01 = __byte_perm(x[0], x[1], 0x5140), ab23 = __byte_perm(x[0], x[1], 0x7362);
-            const uint32_t cd01 = __byte_perm(x[2], x[3], 0x5140), cd23 = __byte_perm(x[2], x[3], 0x7362);
-            raw[4 * h + 0] = __byte_perm(ab01, cd01, 0x5410);
-            raw[4 * h + 1] = __byte_perm(ab01, cd01, 0x7632);
-            raw[4 * h + 2] = __byte_perm(ab23, cd23, 0x5410);
-            raw[4 * h + 3] = __byte_perm(ab23, cd23, 0x7632);
-        }
-        uint32_t cur[8];
-        cur[0] = raw[2];
-        cur[1] = (raw[2] | raw[0]) & ~raw[1];
-        cur[2] = raw[1];
-#pragma unroll
-        for (int b = 0; b < 5; b++) cur[3 + b] = raw[3 + b];
-        // group g (bits [31g, 31g + 31) of the thread's slots) is complete
-        // once the chunk after the one holding its first slot is in
-        if (c >= 1) {
-#pragma unroll
-            for (int g = 0; g < 8; g++) {
-                if (((31 * g) >> 5) == c - 1) {
-                    const int off = (31 * g) & 31;
-#pragma unroll
-                    for (int w = 0; w < 8; w++)
-                        gp[g][w] = (off == 0 ? prev[w] : __funnelshift_r(prev[w], cur[w], off)) & 0x7FFFFFFFu;
-                    cnt[g] = __popc(gp[g][0]) - __popc(gp[g][1]);
-                }
-            }
-        }
-#pragma unroll
-        for (int w = 0; w < 8; w++) prev[w] = cur[w];
-    }
+    mirror_groups(sw, gp, cnt);
     int tot = 0;
 #pragma unroll
     for (int g = 0; g < 8; g++) tot += cnt[g];

@@ -4,7 +4,9 @@
 // tests to check the byte-lane SWAR walk against the oracle without a GPU.
 // With SWAR_MIRROR set, the queries go through the bit-plane mirror instead
 // (mirror_record / mirror_query, the lookup kernel's own functions), falling
-// back to sqf_query_b1 where the two-record window does not decide.
+// back to sqf_query_b1 where the two-record window does not decide.  With
+// SWAR_MIRROR_GROUPS set it checks the build kernel's transposition
+// (mirror_groups) against mirror_record over the whole table instead.
 //   swar_query_host <table.bin> <fps.bin> <q> <r> <nslots> <out.bin>
 #include <cstdio>
 #include <cstdlib>
@@ -39,6 +41,29 @@ int main(int argc, char **argv)
     const size_t n = fpb.size() / 4;
     const uint32_t *fps = reinterpret_cast<const uint32_t *>(fpb.data());
     std::vector<uint32_t> out(n);
+    if (std::getenv("SWAR_MIRROR_GROUPS")) {
+        // the build kernel's per-thread transposition (mirror_groups) against
+        // mirror_record, over every thread range of 31 words (8 groups)
+        const uint32_t ng = gqf::mir_groups(nslots);
+        size_t bad = 0, checked = 0;
+        for (uint32_t t = 0; 8 * t <= ng; t++) {
+            uint64_t sw[gqf::MIR_WORDS];
+            for (uint32_t i = 0; i < gqf::MIR_WORDS; i++) sw[i] = gqf::ld_word(v, gqf::MIR_WORDS * t + i);
+            uint32_t gp[8][8];
+            int cnt[8];
+            gqf::mirror_groups(sw, gp, cnt);
+            for (uint32_t g = 0; g < 8 && 8 * t + g <= ng; g++) {
+                uint32_t r[8];
+                gqf::mirror_record(tab.data(), (uint32_t)tab.size(), 8 * t + g, 0, r);
+                bool ok = cnt[g] == gqf::popc32(r[0]) - gqf::popc32(r[1]);
+                for (int w = 0; w < 8; w++) ok = ok && gp[g][w] == r[w];
+                bad += ok ? 0 : 1;
+                checked++;
+            }
+        }
+        std::fprintf(stderr, "groups checked %zu, differing %zu\n", checked, bad);
+        return bad ? 5 : 0;
+    }
     if (std::getenv("SWAR_MIRROR")) {
         const uint32_t ng = gqf::mir_groups(nslots);
         std::vector<uint32_t> rec((size_t)(ng + 1) * 8);

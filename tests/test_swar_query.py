@@ -136,3 +136,26 @@ def test_mirror_saturated_pending_count(driver, tmp_path):
     assert (want[: fps.size] != 0xFFFFFFFF).all()
     assert np.array_equal(run_driver(driver, tmp_path, t, q, r, probe, mirror=True), want)
     assert ns > 700
+
+
+@pytest.mark.parametrize("q,fill,nodup", [(11, 0.8, True), (13, 0.95, False), (10, 1.0, True)])
+def test_mirror_build_transposition(driver, tmp_path, q, fill, nodup):
+    """The mirror build kernel's per-thread transposition (8x8 bit transposes,
+    a 4x4 byte transpose, funnel shifts into 31-slot groups), compiled for the
+    host, gives every group record exactly as mirror_record does, including
+    the groups past the table's end."""
+    r = 5
+    n = int((1 << q) * fill)
+    keys = O.mt_keys(300 + q, n)
+    if not nodup:
+        keys = np.concatenate([keys, keys[: n // 5]])
+    t = O.sqf_new(q, r)
+    O.sqf_bulk_build(t, q, r, keys, nodup)
+    tf, ff, of = tmp_path / "t.bin", tmp_path / "f.bin", tmp_path / "o.bin"
+    t.tofile(tf)
+    np.zeros(1, np.uint32).tofile(ff)
+    env = dict(os.environ, SWAR_MIRROR_GROUPS="1")
+    p = subprocess.run([driver, str(tf), str(ff), str(q), str(r), str(O.sqf_num_slots(q)), str(of)],
+                       capture_output=True, text=True, env=env)
+    assert p.returncode == 0, p.stderr
+    assert "differing 0" in p.stderr
